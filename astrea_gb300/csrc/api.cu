@@ -1,0 +1,523 @@
+// C ABI (include/astrea_gb300.h): handle management and the step sequence.
+//
+// One step of the core_run loop (astrea.py:66-85) with an s-stage Runge-Kutta
+// scheme is enqueued as:
+//   stage 0:  sweep x -> D_a, sweep y -> D_b (both accumulate eigmax),
+//             dt kernel, combine0 (u, D_a, D_b) -> k1
+//   stage s:  sweep x (state k_s) -> D_a, sweep y (state k_s) fused with the
+//             stage combine -> k_{s+1} (or u after the last stage)
+//   end_step: t += dt, flip the axis order, reset the speed maxima
+// In 1D the single sweep fuses the combine directly.  The HLLC/HLLD axis label
+// of each sweep is read from the device clock's axis order, so one captured
+// graph serves even and odd steps.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/astrea_gb300.h"
+#include "stage.cuh"
+#include "sweep_launch.cuh"
+
+namespace astrea {
+ASTREA_EXTERN_GET_SWEEP(double)
+ASTREA_EXTERN_GET_SWEEP(float)
+}  // namespace astrea
+
+using namespace astrea;
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+static int cuda_fail(cudaError_t e, const char* where) {
+  return fail(ASTREA_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(call)                                        \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+static int stages_of(int integ) {
+  switch (integ) {
+    case EULER: return 1;
+    case SSPRK22: return 2;
+    case SSPRK33: return 3;
+    case SSPRK43: return 4;
+    default: return -1;
+  }
+}
+
+// Event pairs around kernel launches, by kernel kind (astrea_step_timed)
+struct KTimer {
+  std::vector<cudaEvent_t> ev[3][2];
+  int open_kind = -1;
+  cudaError_t start(int kind, cudaStream_t st) {
+    cudaEvent_t e;
+    cudaError_t r = cudaEventCreate(&e);
+    if (r != cudaSuccess) return r;
+    ev[kind][0].push_back(e);
+    open_kind = kind;
+    return cudaEventRecord(e, st);
+  }
+  cudaError_t stop(cudaStream_t st) {
+    cudaEvent_t e;
+    cudaError_t r = cudaEventCreate(&e);
+    if (r != cudaSuccess) return r;
+    ev[open_kind][1].push_back(e);
+    return cudaEventRecord(e, st);
+  }
+  ~KTimer() {
+    for (auto& k : ev)
+      for (auto& v : k)
+        for (auto e : v) cudaEventDestroy(e);
+  }
+};
+#define TSTART(kind) \
+  if (tm) CK(tm->start(kind, st))
+#define TSTOP() \
+  if (tm) CK(tm->stop(st))
+
+struct IEngine {
+  astrea_cfg cfg{};
+  int nv = 0;
+  long long cells = 0;
+  Clock* clk = nullptr;   // [0]: device-time stepping, [1]: explicit-dt (evolve_time / evolve_space)
+  double* part = nullptr; // compensated-sum partials
+  double* sums = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  void* graph_state = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  virtual ~IEngine() {
+    if (graph) cudaGraphExecDestroy(graph);
+    cudaFree(clk);
+    cudaFree(part);
+    cudaFree(sums);
+  }
+  virtual int alloc() = 0;
+  virtual int enqueue_step(void* state, Clock* c, bool device_dt, cudaStream_t st, KTimer* tm = nullptr) = 0;
+  virtual int space(const void* state, int order, void* f0, void* f1, double* eigmax, cudaStream_t st) = 0;
+  virtual int initialise(const void* prim, void* out, cudaStream_t st) = 0;
+  virtual int to_primitive(const void* state, void* out, cudaStream_t st) = 0;
+  virtual int reduce(const void* state, double* host, cudaStream_t st) = 0;
+};
+
+struct astrea_handle {
+  IEngine* eng;
+};
+
+template <typename T> struct Engine final : IEngine {
+  T* k[2] = {nullptr, nullptr};
+  T* d[2] = {nullptr, nullptr};
+  T* tmp = nullptr;
+  SweepFn<T> sweep[2] = {nullptr, nullptr};
+
+  ~Engine() override {
+    for (int i = 0; i < 2; ++i) { cudaFree(k[i]); cudaFree(d[i]); }
+    cudaFree(tmp);
+  }
+
+  long long plane() const { return cells; }
+
+  int alloc() override {
+    const size_t bytes = sizeof(T) * (size_t)nv * (size_t)cells;
+    for (int i = 0; i < 2; ++i) {
+      if (cudaMalloc(&k[i], bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "stage buffer allocation failed");
+      if (cudaMalloc(&d[i], bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "divergence buffer allocation failed");
+    }
+    if (cudaMalloc(&tmp, bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "scratch allocation failed");
+    SweepFn<T> (*getter)(int, int, int, int) = nullptr;
+    switch (cfg.scheme) {
+      case PCM: getter = &get_sweep<T, PCM>; break;
+      case PLM: getter = &get_sweep<T, PLM>; break;
+      case PPM: getter = &get_sweep<T, PPM>; break;
+      case WENO3: getter = &get_sweep<T, WENO3>; break;
+      case WENO5: getter = &get_sweep<T, WENO5>; break;
+      case WENO7: getter = &get_sweep<T, WENO7>; break;
+      default: return fail(ASTREA_ERR_CONFIG, "unknown scheme");
+    }
+    sweep[0] = getter(cfg.model, cfg.solver, cfg.dim, 0);
+    if (cfg.dim == 2) sweep[1] = getter(cfg.model, cfg.solver, cfg.dim, 1);
+    if (!sweep[0] || (cfg.dim == 2 && !sweep[1]))
+      return fail(ASTREA_ERR_CONFIG, "no kernel for this (model, solver, dimension); use model 8 for HLLD or transverse velocities");
+    // set the kernels' shared-memory attribute now, outside any stream capture
+    SweepArgs<T> probe{};
+    probe.n0 = 0;
+    for (int i = 0; i < cfg.dim; ++i) CK(sweep[i](probe, nullptr));
+    return ASTREA_OK;
+  }
+
+  SweepArgs<T> base_args(const T* q, Clock* c) const {
+    SweepArgs<T> a{};
+    a.q = q;
+    a.plane = plane();
+    a.n0 = cfg.n0;
+    a.n1 = cfg.dim == 1 ? 1 : cfg.n1;
+    a.bc = cfg.boundary;
+    a.label = -1;
+    a.limiter = cfg.limiter;
+    a.integ = cfg.integrator;
+    a.gamma = T(cfg.gamma);
+    a.gm1 = T(cfg.gamma - 1.0);
+    a.dx = cfg.dx;
+    a.clock = c;
+    return a;
+  }
+
+  int enqueue_step(void* state, Clock* c, bool device_dt, cudaStream_t st, KTimer* tm = nullptr) override {
+    T* u = static_cast<T*>(state);
+    const int ns = stages_of(cfg.integrator);
+    if (ns < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this build");
+    const long long n = cells;
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>((n + threads - 1) / threads, 152LL * 16);
+    // stage 0
+    {
+      SweepArgs<T> a = base_args(u, c);
+      a.mode = 0;
+      a.want_emax = 1;
+      a.dout = d[0];
+      TSTART(0);
+      CK(sweep[0](a, st));
+      TSTOP();
+      if (cfg.dim == 2) {
+        a.dout = d[1];
+        TSTART(0);
+        CK(sweep[1](a, st));
+        TSTOP();
+      }
+      if (device_dt) {
+        TSTART(2);
+        dt_kernel<<<1, 32, 0, st>>>(c, 1);
+        CK(cudaGetLastError());
+        TSTOP();
+      }
+      T* out0 = ns == 1 ? u : k[0];
+      TSTART(1);
+      combine0_kernel<T><<<blocks, threads, 0, st>>>(u, d[0], cfg.dim == 2 ? d[1] : nullptr, out0, plane(), n, nv,
+                                                     cfg.integrator, c);
+      CK(cudaGetLastError());
+      TSTOP();
+    }
+    for (int s = 1; s < ns; ++s) {
+      T* cur = k[(s - 1) % 2];
+      T* out = s == ns - 1 ? u : k[s % 2];
+      SweepArgs<T> a = base_args(cur, c);
+      a.stage = s;
+      a.u0 = u;
+      a.out = out;
+      if (cfg.dim == 2) {
+        a.mode = 0;
+        a.dout = d[0];
+        TSTART(0);
+        CK(sweep[0](a, st));
+        TSTOP();
+        a.mode = 1;
+        a.dother = d[0];
+        a.dout = nullptr;
+        TSTART(0);
+        CK(sweep[1](a, st));
+        TSTOP();
+      } else {
+        a.mode = 2;
+        TSTART(0);
+        CK(sweep[0](a, st));
+        TSTOP();
+      }
+    }
+    if (device_dt) {
+      TSTART(2);
+      end_step_kernel<<<1, 32, 0, st>>>(c, 1);
+      CK(cudaGetLastError());
+      TSTOP();
+    }
+    return ASTREA_OK;
+  }
+
+  int space(const void* state, int order, void* f0, void* f1, double* eigmax, cudaStream_t st) override {
+    Clock* c = clk + 1;
+    CK(cudaMemsetAsync(&c->emax[0], 0, 2 * sizeof(unsigned long long), st));
+    CK(cudaMemcpyAsync(&c->order, &order, sizeof(int), cudaMemcpyHostToDevice, st));
+    SweepArgs<T> a = base_args(static_cast<const T*>(state), c);
+    a.mode = 0;
+    a.want_emax = 1;
+    a.dout = d[0];
+    a.flux_out = static_cast<T*>(f0);
+    CK(sweep[0](a, st));
+    if (cfg.dim == 2) {
+      a.dout = d[1];
+      a.flux_out = static_cast<T*>(f1);
+      CK(sweep[1](a, st));
+    }
+    unsigned long long e[2];
+    CK(cudaMemcpyAsync(e, &c->emax[0], sizeof(e), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double v[2];
+    std::memcpy(&v[0], &e[0], sizeof(double));
+    std::memcpy(&v[1], &e[1], sizeof(double));
+    if (eigmax) { eigmax[0] = v[0]; eigmax[1] = cfg.dim == 2 ? v[1] : 0.0; }
+    return ASTREA_OK;
+  }
+
+  int initialise(const void* prim, void* out, cudaStream_t st) override {
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>((cells + threads - 1) / threads, 152LL * 16);
+    const int ho = cfg.scheme >= PPM;
+    const T gm1 = T(cfg.gamma - 1.0);
+    const int n1 = cfg.dim == 1 ? 1 : cfg.n1;
+    switch (cfg.model) {
+      case 3: init_pass_a<T, 3><<<blocks, threads, 0, st>>>(static_cast<const T*>(prim), tmp, cfg.n0, n1, plane(), cfg.dim, cfg.boundary, ho, gm1); break;
+      case 4: init_pass_a<T, 4><<<blocks, threads, 0, st>>>(static_cast<const T*>(prim), tmp, cfg.n0, n1, plane(), cfg.dim, cfg.boundary, ho, gm1); break;
+      default: init_pass_a<T, 8><<<blocks, threads, 0, st>>>(static_cast<const T*>(prim), tmp, cfg.n0, n1, plane(), cfg.dim, cfg.boundary, ho, gm1); break;
+    }
+    CK(cudaGetLastError());
+    centre_to_avg_kernel<T><<<blocks, threads, 0, st>>>(tmp, static_cast<T*>(out), cfg.n0, n1, plane(), nv, cfg.dim, cfg.boundary);
+    CK(cudaGetLastError());
+    return ASTREA_OK;
+  }
+
+  int to_primitive(const void* state, void* out, cudaStream_t st) override {
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>((cells + threads - 1) / threads, 152LL * 16);
+    const int ho = cfg.scheme >= PPM;
+    const T gm1 = T(cfg.gamma - 1.0);
+    const int n1 = cfg.dim == 1 ? 1 : cfg.n1;
+    const T* q = static_cast<const T*>(state);
+    T* w = static_cast<T*>(out);
+    switch (cfg.model) {
+      case 3: prim_kernel<T, 3><<<blocks, threads, 0, st>>>(q, w, cfg.n0, n1, plane(), cfg.dim, cfg.boundary, ho, gm1); break;
+      case 4: prim_kernel<T, 4><<<blocks, threads, 0, st>>>(q, w, cfg.n0, n1, plane(), cfg.dim, cfg.boundary, ho, gm1); break;
+      default: prim_kernel<T, 8><<<blocks, threads, 0, st>>>(q, w, cfg.n0, n1, plane(), cfg.dim, cfg.boundary, ho, gm1); break;
+    }
+    CK(cudaGetLastError());
+    return ASTREA_OK;
+  }
+
+  int reduce(const void* state, double* host, cudaStream_t st) override {
+    const int nb = 152;
+    sums_pass1<T><<<nb, 256, 0, st>>>(static_cast<const T*>(state), plane(), cells, nv, part);
+    CK(cudaGetLastError());
+    sums_pass2<<<1, 32, 0, st>>>(part, nb, nv, sums);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, sums, sizeof(double) * nv, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return ASTREA_OK;
+  }
+};
+
+static int validate(const astrea_cfg* c) {
+  if (!c) return fail(ASTREA_ERR_ARG, "cfg is NULL");
+  if (c->dim != 1 && c->dim != 2) return fail(ASTREA_ERR_CONFIG, "dim must be 1 or 2");
+  if (c->n0 < 4 || (c->dim == 2 && c->n1 < 4)) return fail(ASTREA_ERR_CONFIG, "at least 4 cells per axis are required");
+  if (c->dim == 1 && c->n1 != 1) return fail(ASTREA_ERR_CONFIG, "1D grids have n1 == 1");
+  if (c->model != 3 && c->model != 4 && c->model != 8) return fail(ASTREA_ERR_CONFIG, "model must be 3, 4 or 8");
+  if (c->model == 3 && c->dim != 1) return fail(ASTREA_ERR_CONFIG, "model 3 is 1D only");
+  if (c->model == 4 && c->dim != 2) return fail(ASTREA_ERR_CONFIG, "model 4 is 2D only");
+  if (c->precision != 32 && c->precision != 64) return fail(ASTREA_ERR_CONFIG, "precision must be 32 or 64");
+  if (c->scheme < 0 || c->scheme > WENO7) return fail(ASTREA_ERR_CONFIG, "unknown scheme");
+  if (c->solver < 0 || c->solver > HLLD) return fail(ASTREA_ERR_CONFIG, "unknown solver");
+  if (stages_of(c->integrator) < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this build");
+  if (c->boundary != EDGE && c->boundary != WRAP) return fail(ASTREA_ERR_CONFIG, "boundary must be edge(0) or wrap(1)");
+  if (!(c->dx > 0) || !(c->cfl > 0) || !(c->gamma > 1) || c->checkpoints < 1)
+    return fail(ASTREA_ERR_CONFIG, "dx, cfl > 0, gamma > 1, checkpoints >= 1 required");
+  if ((long long)c->n0 * (long long)(c->dim == 2 ? c->n1 : 1) > (1LL << 31))
+    return fail(ASTREA_ERR_CONFIG, "grid larger than 2^31 cells");
+  return ASTREA_OK;
+}
+
+extern "C" {
+
+int astrea_version(void) { return 100; }
+
+const char* astrea_last_error(void) { return g_last_error.c_str(); }
+
+int astrea_create(const astrea_cfg* cfg, astrea_handle** out) {
+  if (!out) return fail(ASTREA_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  IEngine* e = cfg->precision == 64 ? static_cast<IEngine*>(new Engine<double>()) : static_cast<IEngine*>(new Engine<float>());
+  e->cfg = *cfg;
+  if (cfg->dim == 1) e->cfg.n1 = 1;
+  e->nv = cfg->model;
+  e->cells = (long long)cfg->n0 * (cfg->dim == 2 ? cfg->n1 : 1);
+  if (cudaMalloc(&e->clk, 2 * sizeof(Clock)) != cudaSuccess || cudaMalloc(&e->part, 152 * 8 * 2 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&e->sums, 8 * sizeof(double)) != cudaSuccess) {
+    delete e;
+    return fail(ASTREA_ERR_OOM, "clock allocation failed");
+  }
+  rc = e->alloc();
+  if (rc) {
+    delete e;
+    return rc;
+  }
+  astrea_handle* h = new astrea_handle{e};
+  rc = astrea_reset_clock(h, 0.0, 1, 0, nullptr);
+  if (rc) {
+    delete e;
+    delete h;
+    return rc;
+  }
+  CK(cudaDeviceSynchronize());
+  *out = h;
+  return ASTREA_OK;
+}
+
+void astrea_destroy(astrea_handle* h) {
+  if (!h) return;
+  delete h->eng;
+  delete h;
+}
+
+int astrea_layout(const astrea_handle* h, int* nv, long long* cells) {
+  if (!h) return fail(ASTREA_ERR_ARG, "handle is NULL");
+  if (nv) *nv = h->eng->nv;
+  if (cells) *cells = h->eng->cells;
+  return ASTREA_OK;
+}
+
+int astrea_initialise(astrea_handle* h, const void* prim, void* state_out, void* stream) {
+  if (!h || !prim || !state_out) return fail(ASTREA_ERR_ARG, "NULL argument");
+  return h->eng->initialise(prim, state_out, static_cast<cudaStream_t>(stream));
+}
+
+int astrea_reset_clock(astrea_handle* h, double t, int idx, int order, void* stream) {
+  if (!h) return fail(ASTREA_ERR_ARG, "handle is NULL");
+  IEngine* e = h->eng;
+  Clock c[2];
+  std::memset(c, 0, sizeof(c));
+  for (int i = 0; i < 2; ++i) {
+    c[i].t = t;
+    c[i].dt = 0.0;
+    c[i].t_end = e->cfg.t_end;
+    c[i].chkpt = e->cfg.t_end / e->cfg.checkpoints;
+    c[i].cfl = e->cfg.cfl;
+    c[i].dx = e->cfg.dx;
+    c[i].idx = idx;
+    c[i].order = e->cfg.dim == 2 ? (order & 1) : 0;
+    c[i].naxes = e->cfg.dim;
+    c[i].done = 0;
+  }
+  c[0].done = !(t < e->cfg.t_end);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CK(cudaMemcpyAsync(e->clk, c, sizeof(c), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  return ASTREA_OK;
+}
+
+int astrea_step(astrea_handle* h, void* state, int nsteps, void* stream) {
+  if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  for (int i = 0; i < nsteps; ++i) {
+    int rc = h->eng->enqueue_step(state, h->eng->clk, true, st);
+    if (rc) return rc;
+  }
+  return ASTREA_OK;
+}
+
+int astrea_step_timed(astrea_handle* h, void* state, int nsteps, double* kernel_ms, int* launches, void* stream) {
+  if (!h || !state || !kernel_ms || !launches) return fail(ASTREA_ERR_ARG, "NULL argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  KTimer tm;
+  for (int i = 0; i < nsteps; ++i) {
+    int rc = h->eng->enqueue_step(state, h->eng->clk, true, st, &tm);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(st));
+  for (int k = 0; k < 3; ++k) {
+    double ms = 0.0;
+    for (size_t i = 0; i < tm.ev[k][0].size(); ++i) {
+      float x = 0.f;
+      CK(cudaEventElapsedTime(&x, tm.ev[k][0][i], tm.ev[k][1][i]));
+      ms += x;
+    }
+    kernel_ms[k] = ms;
+    launches[k] = (int)tm.ev[k][0].size();
+  }
+  return ASTREA_OK;
+}
+
+int astrea_graph_step(astrea_handle* h, void* state, int nsteps, void* stream) {
+  if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
+  IEngine* e = h->eng;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!e->graph || e->graph_state != state) {
+    if (e->graph) {
+      cudaGraphExecDestroy(e->graph);
+      e->graph = nullptr;
+    }
+    cudaStream_t cap;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed));
+    int rc = e->enqueue_step(state, e->clk, true, cap);
+    cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&e->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+    e->graph_state = state;
+  }
+  for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(e->graph, st));
+  return ASTREA_OK;
+}
+
+int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* done, int* status, void* stream) {
+  if (!h) return fail(ASTREA_ERR_ARG, "handle is NULL");
+  Clock c;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CK(cudaMemcpyAsync(&c, h->eng->clk, sizeof(Clock), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (t) *t = c.t;
+  if (dt) *dt = c.dt;
+  if (steps) *steps = c.steps;
+  if (done) *done = c.done;
+  if (status) *status = c.status;
+  return ASTREA_OK;
+}
+
+int astrea_space(astrea_handle* h, const void* state, int order, void* flux_ax0, void* flux_ax1, double* eigmax,
+                 void* stream) {
+  if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
+  return h->eng->space(state, order & 1, flux_ax0, flux_ax1, eigmax, static_cast<cudaStream_t>(stream));
+}
+
+int astrea_time(astrea_handle* h, void* state, double dt, int order, void* stream) {
+  if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
+  IEngine* e = h->eng;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  Clock c;
+  std::memset(&c, 0, sizeof(c));
+  c.t = 0.0;
+  c.dt = dt;
+  c.t_end = 1e300;
+  c.chkpt = 1e300;
+  c.cfl = e->cfg.cfl;
+  c.dx = e->cfg.dx;
+  c.idx = 1;
+  c.order = e->cfg.dim == 2 ? (order & 1) : 0;
+  c.naxes = e->cfg.dim;
+  CK(cudaMemcpyAsync(e->clk + 1, &c, sizeof(c), cudaMemcpyHostToDevice, st));
+  int rc = e->enqueue_step(state, e->clk + 1, false, st);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(st));
+  return ASTREA_OK;
+}
+
+int astrea_to_primitive(astrea_handle* h, const void* state, void* prim_out, void* stream) {
+  if (!h || !state || !prim_out) return fail(ASTREA_ERR_ARG, "NULL argument");
+  return h->eng->to_primitive(state, prim_out, static_cast<cudaStream_t>(stream));
+}
+
+int astrea_reduce_conserved(astrea_handle* h, const void* state, double* sums_host, void* stream) {
+  if (!h || !state || !sums_host) return fail(ASTREA_ERR_ARG, "NULL argument");
+  return h->eng->reduce(state, sums_host, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

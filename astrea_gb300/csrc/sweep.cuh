@@ -1,0 +1,463 @@
+// The sweep kernel: one axis of the spatial operator for one tile of the grid.
+//
+// A CTA owns TS cells along the sweep axis and TT rows across it.  It stages
+// the conservative state of the tile plus halos in shared memory and computes,
+// level by level, every intermediate the reference builds with whole-array
+// NumPy for that axis (schemes/*.run, solvers.calculate_Riemann_flux):
+//
+//   q  -> wS (cell-averaged primitives, 2nd or 4th order)      fv.py:89-143
+//      -> (wL, wR) face values per cell (PCM/PLM/PPM/WENO)      schemes/*, limiters.py
+//      -> interface speeds lambda of the interface averages      fv.compute_eigen
+//      -> face-averaged Riemann flux F_avg                         solvers.py:39-42
+//      -> [2D] face-centred states, second solve, F_c - d2 F_avg  solvers.py:44-57
+//      -> divergence (F[i+1]-F[i])/dx                              evolvers.py:41-49
+//
+// and then either stores the divergence (first sweep of a stage) or adds the
+// other sweep's divergence and applies the Runge-Kutta stage combine
+// (last sweep of a stage).  Every level is held at *virtual* indices; an
+// access at virtual v of a level is served by the value at rho(v) (clamp for
+// outflow), which is the reference's per-intermediate np.pad.
+#pragma once
+#include "physics.cuh"
+#include "recon.cuh"
+
+namespace astrea {
+
+constexpr double C24 = 1.0 / 24.0;
+
+template <typename T> struct SweepArgs {
+  const T* q;         // stage input state, NV planes
+  long long plane;    // plane stride (elements)
+  int n0, n1;         // grid extents: axis 0 (x), axis 1 (y, contiguous); 1D: n0 = N, n1 = 1
+  int bc;
+  int label;          // HLLC/HLLD axis label (iteration position); < 0: from the clock's axis order
+  int limiter;        // PLM slope limiter: 0 minmod, 1 superbee
+  int mode;           // 0: store divergence, 1: add other divergence + combine, 2: combine (sole sweep)
+  int integ, stage;   // Runge-Kutta scheme and stage for the combine
+  int want_emax;      // accumulate the max wave speed of this axis into the clock
+  T gamma, gm1;
+  double dx;
+  T* dout;            // mode 0: divergence output (NV planes)
+  const T* dother;    // mode 1: divergence of the other sweep
+  const T* u0;        // step-start state
+  T* out;             // combine output
+  Clock* clock;
+  T* flux_out;        // optional: interface fluxes [NV][Ns+1][Nt]
+};
+
+template <int SCH, int DIM, int TS, int TT> struct Geom {
+  static constexpr bool HO = SCH >= PPM;  // 4th-order conversions (generic.py:250-255)
+  static constexpr bool ROE = SCH >= PPM; // Roe-type interface average for the wave speed
+  // sweep-axis ranges [s0+BEG, s0+TS+END) of each level
+  static constexpr int R_BEG = -1, R_END = 2;
+  static constexpr int W_BEG = R_BEG - Reach<SCH>::L, W_END = R_END + Reach<SCH>::R;
+  static constexpr int Q_BEG = W_BEG - (HO ? 1 : 0), Q_END = W_END + (HO ? 1 : 0);
+  static constexpr int QW = TS + Q_END - Q_BEG, WW = TS + W_END - W_BEG, RW = TS + R_END - R_BEG;
+  static constexpr int YW = TS + 2;  // lambda of the interface averages right of cells s0-1 .. s0+TS
+  static constexpr int KW = TS + 1;  // interfaces s0 .. s0+TS
+  // transverse halos (2D): rows [t0-H, t0+TT+H)
+  static constexpr int FT = DIM == 2 ? 1 : 0;
+  static constexpr int RT = DIM == 2 ? (HO ? 2 : 1) : 0;
+  static constexpr int WT = RT;
+  static constexpr int QT = DIM == 2 ? (HO ? 3 : 1) : 0;
+  static constexpr int QH = TT + 2 * QT, WH = TT + 2 * WT, RH = TT + 2 * RT, FH = TT + 2 * FT;
+};
+
+template <int SCH, int DIM, int TS, int TT, int NV> struct Smem {
+  using G = Geom<SCH, DIM, TS, TT>;
+  static constexpr int n_q = NV * G::QH * G::QW;
+  static constexpr int n_qw = G::HO ? n_q : 0;
+  static constexpr int n_face = DIM == 2 ? 5 * NV * G::FH * G::KW : 0;
+  static constexpr int n_F = NV * TT * G::KW;
+  // the face arrays reuse the q level once it is dead; PCM reads raw q on faces, so it keeps q
+  static constexpr int FA_OFF = SCH == PCM ? n_q : 0;
+  static constexpr int n_region0 = (n_q + n_qw) > (FA_OFF + n_face + n_F) ? (n_q + n_qw) : (FA_OFF + n_face + n_F);
+  static constexpr int n_w = NV * G::WH * G::WW;
+  static constexpr int n_R = 2 * NV * G::RH * G::RW;
+  static constexpr int n_lam = G::FH * G::YW;
+  static constexpr int total = n_region0 + n_w + n_R + n_lam + 64;
+};
+
+template <class M, typename T> __device__ __forceinline__ void load_sm(const T* base, int stride, int idx, T* x) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = T(0);
+#pragma unroll
+  for (int s = 0; s < M::NV; ++s) x[M::var(s)] = base[s * stride + idx];
+}
+template <class M, typename T> __device__ __forceinline__ void store_sm(T* base, int stride, int idx, const T* x) {
+#pragma unroll
+  for (int s = 0; s < M::NV; ++s) base[s * stride + idx] = x[M::var(s)];
+}
+
+// Stage combines (evolvers.py:150-185), with the reference's operation order
+template <typename T> __device__ __forceinline__ T combine(int integ, int stage, T u, T cur, T L, T dt) {
+  switch (integ) {
+    case SSPRK33:
+      if (stage == 0) return u + dt * L;
+      if (stage == 1) return T(.25) * ((T(3) * u + cur) + dt * L);
+      return T(1.0 / 3.0) * ((u + T(2) * cur) + (T(2) * dt) * L);
+    case SSPRK22:
+      if (stage == 0) return u + dt * L;
+      return T(.5) * ((u + cur) + dt * L);
+    case SSPRK43:
+      if (stage == 0) return u + (T(.5) * dt) * L;
+      if (stage == 1) return cur + (T(.5) * dt) * L;
+      if (stage == 2) return T(1.0 / 6.0) * ((T(4) * u + T(2) * cur) + dt * L);
+      return cur + (T(.5) * dt) * L;
+    default:  // forward Euler
+      return u + dt * L;
+  }
+}
+
+template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, unsigned long long* dst) {
+  __shared__ double red[32];
+  double x = (double)v;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = npmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    double y = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) y = npmax(y, __shfl_xor_sync(0xffffffffu, y, o));
+    if (lane == 0) atomicMax(dst, (unsigned long long)__double_as_longlong(y));
+  }
+}
+
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT>
+__global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
+  using M = Model<MID>;
+  using G = Geom<SCH, DIM, TS, TT>;
+  using S = Smem<SCH, DIM, TS, TT, M::NV>;
+  constexpr int NV = M::NV;
+  if (a.clock->done) return;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  T* s_q = sm;                       // region 0 (a): q and its point primitives
+  T* s_qw = s_q + S::n_q;
+  T* s_fa = sm + S::FA_OFF;          // region 0 (b): face arrays (2D) and F
+  T* s_F = s_fa + S::n_face;
+  T* s_w = sm + S::n_region0;
+  T* s_R = s_w + S::n_w;
+  T* s_lam = s_R + S::n_R;
+
+  const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
+  const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
+  const int s0 = blockIdx.x * TS;
+  const int t0 = blockIdx.y * TT;
+  const Clamp rs_ = make_rho(a.bc, Ns);
+  const Clamp rt_ = make_rho(a.bc, Nt);
+  const T gamma = a.gamma, gm1 = a.gm1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  // axis label of this sweep: its position in the step's iteration order
+  const int label = a.label >= 0 ? a.label : (DIM == 1 ? 0 : (AX == 0 ? a.clock->order : 1 - a.clock->order));
+
+  auto gidx = [&](int gs, int gt) -> long long {
+    if (DIM == 1) return gs;
+    return AX == 0 ? (long long)gs * a.n1 + gt : (long long)gt * a.n1 + gs;
+  };
+
+  // ---- level q: conservative state with halos (input boundary map), and its point primitives
+  {
+    constexpr int W = G::QW, H = G::QH;
+    for (int e = tid; e < W * H; e += nth) {
+      int row, col;
+      if (DIM == 2 && AX == 0) { row = e % H; col = e / H; } else { col = e % W; row = e / W; }
+      const int vs = s0 + G::Q_BEG + col, vt = t0 - G::QT + row;
+      const int gs = bc_map(vs, Ns, a.bc), gt = DIM == 2 ? bc_map(vt, Nt, a.bc) : 0;
+      const long long g = gidx(gs, gt);
+      T q[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) q[i] = T(0);
+#pragma unroll
+      for (int s = 0; s < NV; ++s) q[M::var(s)] = a.q[s * a.plane + g];
+      const int li = row * W + col;
+      store_sm<M>(s_q, H * W, li, q);
+      if constexpr (G::HO) {
+        T w[8];
+        c2p<M>(q, w, gm1);
+        store_sm<M>(s_qw, H * W, li, w);
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- level wS: cell-averaged primitives
+  {
+    constexpr int W = G::WW, H = G::WH, QW = G::QW, QH = G::QH;
+    for (int e = tid; e < W * H; e += nth) {
+      const int row = e / W, col = e % W;
+      const int vs = s0 + G::W_BEG + col, vt = t0 - G::WT + row;
+      const int rs = rs_(vs), rt = DIM == 2 ? rt_(vt) : 0;
+      const int qc = rs - (s0 + G::Q_BEG), qr = rt - (t0 - G::QT);
+      T w[8];
+      if constexpr (G::HO) {
+        // fv.high_order_convert_conservative: sweep axis first, then transverse (fv.py:126-143)
+        const int qcm = rs_(rs - 1) - (s0 + G::Q_BEG), qcp = rs_(rs + 1) - (s0 + G::Q_BEG);
+        T qq[8], wc[8];
+        T q0[8], qm[8], qp[8], w0[8], wm[8], wp[8];
+        load_sm<M>(s_q, QH * QW, qr * QW + qc, q0);
+        load_sm<M>(s_q, QH * QW, qr * QW + qcm, qm);
+        load_sm<M>(s_q, QH * QW, qr * QW + qcp, qp);
+        load_sm<M>(s_qw, QH * QW, qr * QW + qc, w0);
+        load_sm<M>(s_qw, QH * QW, qr * QW + qcm, wm);
+        load_sm<M>(s_qw, QH * QW, qr * QW + qcp, wp);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          qq[i] = q0[i] - T(C24) * ((qp[i] - q0[i]) - (q0[i] - qm[i]));
+          wc[i] = T(C24) * ((wp[i] - w0[i]) - (w0[i] - wm[i]));
+        }
+        if constexpr (DIM == 2) {
+          const int qrm = rt_(rt - 1) - (t0 - G::QT), qrp = rt_(rt + 1) - (t0 - G::QT);
+          load_sm<M>(s_q, QH * QW, qrm * QW + qc, qm);
+          load_sm<M>(s_q, QH * QW, qrp * QW + qc, qp);
+          load_sm<M>(s_qw, QH * QW, qrm * QW + qc, wm);
+          load_sm<M>(s_qw, QH * QW, qrp * QW + qc, wp);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            qq[i] = qq[i] - T(C24) * ((qp[i] - q0[i]) - (q0[i] - qm[i]));
+            wc[i] = wc[i] + T(C24) * ((wp[i] - w0[i]) - (w0[i] - wm[i]));
+          }
+        }
+        c2p<M>(qq, w, gm1);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) w[i] = w[i] + wc[i];
+      } else {
+        T q0[8];
+        load_sm<M>(s_q, QH * QW, qr * QW + qc, q0);
+        c2p<M>(q0, w, gm1);
+      }
+      store_sm<M>(s_w, H * W, row * W + col, w);
+    }
+  }
+  __syncthreads();
+
+  // ---- level R: reconstructed face values (wL at i-1/2, wR at i+1/2) of each cell
+  {
+    constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
+    for (int e = tid; e < W * H * NV; e += nth) {
+      const int s = e / (W * H), rem = e % (W * H);
+      const int row = rem / W, col = rem % W;
+      const int vs = s0 + G::R_BEG + col, vt = t0 - G::RT + row;
+      const int rs = rs_(vs), rt = DIM == 2 ? rt_(vt) : 0;
+      const T* wrow = s_w + (s * WH + (rt - (t0 - G::WT))) * WW - (s0 + G::W_BEG);
+      auto at = [&](int x) -> T { return wrow[x]; };
+      T wl, wr;
+      reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr);
+      s_R[((0 * NV + s) * H + row) * W + col] = wl;
+      s_R[((1 * NV + s) * H + row) * W + col] = wr;
+    }
+  }
+  __syncthreads();
+
+  // accessors into the R level: virtual cell x (already mapped), real row rt
+  auto loadL = [&](int x, int rt, T* out) {
+    load_sm<M>(s_R, G::RH * G::RW, (rt - (t0 - G::RT)) * G::RW + (x - (s0 + G::R_BEG)), out);
+  };
+  auto loadR = [&](int x, int rt, T* out) {
+    load_sm<M>(s_R + NV * G::RH * G::RW, G::RH * G::RW, (rt - (t0 - G::RT)) * G::RW + (x - (s0 + G::R_BEG)), out);
+  };
+
+  // ---- level lambda: wave speed of the interface average right of each cell (fv.compute_eigen)
+  {
+    constexpr int W = G::YW, H = G::FH;
+    T lmax = T(0);
+    for (int e = tid; e < W * H; e += nth) {
+      const int row = e / W, col = e % W;
+      const int vj = s0 - 1 + col, vt = t0 - G::FT + row;
+      const int rj = rs_(vj), rt = DIM == 2 ? rt_(vt) : 0;
+      T y[8];
+      if constexpr (SCH == PCM) {
+        load_sm<M>(s_w, G::WH * G::WW, (rt - (t0 - G::WT)) * G::WW + (rj - (s0 + G::W_BEG)), y);
+      } else {
+        T wp[8], wm[8];
+        loadL(rs_(rj + 1), rt, wp);
+        loadR(rj, rt, wm);
+        if constexpr (G::ROE) roe_avg<M>(wp, wm, y);
+        else arith_avg<M>(wp, wm, y);
+      }
+      const T lam = max_speed<M, DIM == 1 ? 0 : AX>(y, gamma);
+      s_lam[row * W + col] = lam;
+      if (a.want_emax && vj >= s0 && vj < s0 + TS && vj < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) lmax = npmax(lmax, lam);
+    }
+    if (a.want_emax) block_max_to_clock(lmax, &a.clock->emax[DIM == 1 ? 0 : AX]);
+  }
+  __syncthreads();
+
+  // per-interface solve from the six face arrays
+  auto solve = [&](int k_local, int lam_row, const T* wSr, const T* wp, const T* wm, const T* qp, const T* qm,
+                   const T* fp, const T* fm, T* F) {
+    if constexpr (SOL == LLF) {
+      const T alpha = npmax(s_lam[lam_row * G::YW + k_local], s_lam[lam_row * G::YW + k_local + 1]);
+      llf<M>(alpha, qp, qm, fp, fm, F);
+    } else if constexpr (SOL == HLLC) {
+      hllc<M>(label, gamma, wp, wm, qp, qm, fp, fm, F);
+    } else {
+      hlld<T>(label, gamma, wSr, wp, wm, qp, qm, fp, fm, F);
+    }
+  };
+  auto load_wS = [&](int x, int rt, T* out) {
+    load_sm<M>(s_w, G::WH * G::WW, (rt - (t0 - G::WT)) * G::WW + (x - (s0 + G::W_BEG)), out);
+  };
+  // face states of interface vk at real row rt
+  auto face_states = [&](int vk, int rt, T* wp, T* wm) {
+    loadL(rs_(vk), rt, wp);
+    loadR(rs_(vk - 1), rt, wm);
+  };
+  // conservative face state (plus side: cells' left faces; minus side: right faces)
+  auto face_cons = [&](int vk, int rt, const T* w, bool plus, T* q) {
+    if constexpr (SCH == PCM) {
+      // pcm.py:85-99: raw cell averages
+      const int x = plus ? rs_(vk) : rs_(vk - 1);
+      load_sm<M>(s_q, G::QH * G::QW, (rt - (t0 - G::QT)) * G::QW + (x - (s0 + G::Q_BEG)), q);
+    } else if constexpr (G::HO && DIM == 2) {
+      // fv.high_order_convert_primitive on a face array: transverse axis only (fv.py:105-122)
+      const int rm = rt_(rt - 1), rp = rt_(rt + 1);
+      T wm_[8], wp_[8], tmp[8];
+      if (plus) { loadL(rs_(vk), rm, wm_); loadL(rs_(vk), rp, wp_); }
+      else { loadR(rs_(vk - 1), rm, wm_); loadR(rs_(vk - 1), rp, wp_); }
+      T ww[8], qc[8], qm_[8], qp_[8], q0[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) ww[i] = w[i] - T(C24) * ((wp_[i] - w[i]) - (w[i] - wm_[i]));
+      p2c<M>(w, q0, gm1);
+      p2c<M>(wm_, qm_, gm1);
+      p2c<M>(wp_, qp_, gm1);
+      p2c<M>(ww, tmp, gm1);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        qc[i] = T(C24) * ((qp_[i] - q0[i]) - (q0[i] - qm_[i]));
+        q[i] = tmp[i] + qc[i];
+      }
+    } else {
+      p2c<M>(w, q, gm1);
+    }
+  };
+
+  if constexpr (DIM == 1) {
+    // ---- 1D: single solve per interface
+    constexpr int W = G::KW;
+    for (int e = tid; e < W; e += nth) {
+      const int vk = s0 + e;
+      if (vk > Ns) continue;
+      T wp[8], wm[8], qp[8], qm[8], fp[8], fm[8], F[8], wSr[8];
+      face_states(vk, 0, wp, wm);
+      face_cons(vk, 0, wp, true, qp);
+      face_cons(vk, 0, wm, false, qm);
+      make_flux<M, 0>(wp, fp, gamma, gm1);
+      make_flux<M, 0>(wm, fm, gamma, gm1);
+      if constexpr (SOL == HLLD) load_wS(rs_(vk), 0, wSr);
+      solve(e, 0, wSr, wp, wm, qp, qm, fp, fm, F);
+      store_sm<M>(s_F, TT * W, e, F);
+    }
+  } else {
+    // ---- 2D level A: face-averaged solve on rows t0-1 .. t0+TT
+    constexpr int W = G::KW, H = G::FH;
+    T* s_qp = s_fa;
+    T* s_qm = s_fa + NV * H * W;
+    T* s_fp = s_fa + 2 * NV * H * W;
+    T* s_fm = s_fa + 3 * NV * H * W;
+    T* s_Fa = s_fa + 4 * NV * H * W;
+    for (int e = tid; e < W * H; e += nth) {
+      const int row = e / W, col = e % W;
+      const int vk = s0 + col, vt = t0 - G::FT + row;
+      if (vk > Ns) continue;
+      const int rt = rt_(vt);
+      T wp[8], wm[8], qp[8], qm[8], fp[8], fm[8], F[8], wSr[8];
+      face_states(vk, rt, wp, wm);
+      face_cons(vk, rt, wp, true, qp);
+      face_cons(vk, rt, wm, false, qm);
+      make_flux<M, AX>(wp, fp, gamma, gm1);
+      make_flux<M, AX>(wm, fm, gamma, gm1);
+      if constexpr (SOL == HLLD) load_wS(rs_(vk), rt, wSr);
+      solve(col, row, wSr, wp, wm, qp, qm, fp, fm, F);
+      const int li = row * W + col;
+      store_sm<M>(s_qp, H * W, li, qp);
+      store_sm<M>(s_qm, H * W, li, qm);
+      store_sm<M>(s_fp, H * W, li, fp);
+      store_sm<M>(s_fm, H * W, li, fm);
+      store_sm<M>(s_Fa, H * W, li, F);
+    }
+    __syncthreads();
+    // ---- 2D level B: face-centred states (fv.high_order_convert 'avg'/'face'), second solve, F_c - d2 F_avg
+    for (int e = tid; e < W * TT; e += nth) {
+      const int row = e / W, col = e % W;
+      const int vk = s0 + col, vt = t0 + row;
+      if (vk > Ns) continue;
+      const int rt = rt_(vt), rm = rt_(rt - 1), rp = rt_(rt + 1);
+      const int fr = rt - (t0 - G::FT), frm = rm - (t0 - G::FT), frp = rp - (t0 - G::FT);
+      T x0[8], xm[8], xp[8];
+      T cwp[8], cwm[8], cqp[8], cqm[8], cfp[8], cfm[8], Fc[8], wSr[8];
+      auto conv = [&](T* out) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) out[i] = x0[i] - T(C24) * ((xp[i] - x0[i]) - (x0[i] - xm[i]));
+      };
+      loadL(rs_(vk), rt, x0); loadL(rs_(vk), rm, xm); loadL(rs_(vk), rp, xp);
+      conv(cwp);
+      loadR(rs_(vk - 1), rt, x0); loadR(rs_(vk - 1), rm, xm); loadR(rs_(vk - 1), rp, xp);
+      conv(cwm);
+      load_sm<M>(s_qp, H * W, fr * W + col, x0); load_sm<M>(s_qp, H * W, frm * W + col, xm); load_sm<M>(s_qp, H * W, frp * W + col, xp);
+      conv(cqp);
+      load_sm<M>(s_qm, H * W, fr * W + col, x0); load_sm<M>(s_qm, H * W, frm * W + col, xm); load_sm<M>(s_qm, H * W, frp * W + col, xp);
+      conv(cqm);
+      load_sm<M>(s_fp, H * W, fr * W + col, x0); load_sm<M>(s_fp, H * W, frm * W + col, xm); load_sm<M>(s_fp, H * W, frp * W + col, xp);
+      conv(cfp);
+      load_sm<M>(s_fm, H * W, fr * W + col, x0); load_sm<M>(s_fm, H * W, frm * W + col, xm); load_sm<M>(s_fm, H * W, frp * W + col, xp);
+      conv(cfm);
+      if constexpr (SOL == HLLD) load_wS(rs_(vk), rt, wSr);
+      solve(col, fr, wSr, cwp, cwm, cqp, cqm, cfp, cfm, Fc);
+      load_sm<M>(s_Fa, H * W, fr * W + col, x0); load_sm<M>(s_Fa, H * W, frm * W + col, xm); load_sm<M>(s_Fa, H * W, frp * W + col, xp);
+      T F[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) F[i] = Fc[i] - T(C24) * ((xp[i] - x0[i]) - (x0[i] - xm[i]));
+      store_sm<M>(s_F, TT * W, row * W + col, F);
+    }
+  }
+  __syncthreads();
+
+  // ---- optional: interface fluxes for the evolve_space interface
+  if (a.flux_out) {
+    constexpr int W = G::KW;
+    for (int e = tid; e < W * TT; e += nth) {
+      const int row = e / W, col = e % W;
+      const int vk = s0 + col, vt = t0 + row;
+      if (vk > Ns || vt >= Nt) continue;
+      if (col == TS && vk != Ns) continue;  // interface s0+TS belongs to the next tile
+      const long long fidx = (long long)vk * Nt + vt;
+      const long long fplane = (long long)(Ns + 1) * Nt;
+#pragma unroll
+      for (int s = 0; s < NV; ++s) a.flux_out[s * fplane + fidx] = s_F[(s * TT + row) * W + col];
+    }
+  }
+
+  // ---- divergence and stage combine on the tile's own cells
+  {
+    constexpr int W = G::KW;
+    const T dxT = T(a.dx);
+    const T dtT = T(a.clock->dt);
+    for (int e = tid; e < TS * TT; e += nth) {
+      int row, col;
+      if (DIM == 2 && AX == 0) { row = e % TT; col = e / TT; } else { col = e % TS; row = e / TS; }
+      const int vs = s0 + col, vt = t0 + row;
+      if (vs >= Ns || vt >= Nt) continue;
+      const long long g = gidx(vs, vt);
+#pragma unroll
+      for (int s = 0; s < NV; ++s) {
+        const T D = (s_F[(s * TT + row) * W + col + 1] - s_F[(s * TT + row) * W + col]) / dxT;
+        if (a.mode == 0) {
+          a.dout[s * a.plane + g] = D;
+        } else {
+          const T total = a.mode == 1 ? a.dother[s * a.plane + g] + D : D;
+          const T L = -total;
+          const T u = a.u0[s * a.plane + g];
+          const T cur = a.q[s * a.plane + g];
+          a.out[s * a.plane + g] = combine<T>(a.integ, a.stage, u, cur, L, dtT);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace astrea

@@ -1,0 +1,76 @@
+// Launchers for the sweep kernel and the (precision, scheme) dispatch tables.
+// Each sweep_<prec>_<scheme>.cu translation unit instantiates get_sweep for one
+// (precision, scheme) pair so the build compiles them in parallel.
+#pragma once
+#include "sweep.cuh"
+
+namespace astrea {
+
+template <typename T> using SweepFn = cudaError_t (*)(const SweepArgs<T>&, cudaStream_t);
+
+// tiles: 1D 32 cells x 64 threads; 2D 32 (sweep) x 8 (rows) x 256 threads
+constexpr int TS1 = 32, NT1 = 64;
+constexpr int TS2 = 32, TT2 = 8, NT2 = 256;
+
+template <typename T, int MID, int SCH, int DIM> constexpr size_t sweep_smem_bytes() {
+  constexpr int TS = DIM == 1 ? TS1 : TS2, TT = DIM == 1 ? 1 : TT2;
+  return sizeof(T) * (size_t)Smem<SCH, DIM, TS, TT, Model<MID>::NV>::total;
+}
+
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX>
+cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
+  constexpr int TS = DIM == 1 ? TS1 : TS2, TT = DIM == 1 ? 1 : TT2, NT = DIM == 1 ? NT1 : NT2;
+  constexpr size_t bytes = sweep_smem_bytes<T, MID, SCH, DIM>();
+  static_assert(bytes <= 227 * 1024, "sweep tile exceeds the shared memory of one CTA");
+  auto k = sweep_kernel<T, MID, SCH, SOL, DIM, AX, TS, TT>;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static unsigned long long configured = 0ull;  // one bit per device
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(configured & bit)) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    configured |= bit;
+  }
+  if (a.n0 <= 0) return cudaSuccess;  // configure-only call (before any graph capture)
+  const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
+  const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
+  dim3 grid((Ns + TS - 1) / TS, (Nt + TT - 1) / TT);
+  k<<<grid, NT, bytes, st>>>(a);
+  return cudaGetLastError();
+}
+
+// Supported (model, solver) pairs: Euler models with LLF/HLLC, the 8-variable
+// model with LLF/HLLC/HLLD.
+template <typename T, int SCH> SweepFn<T> get_sweep(int mid, int sol, int dim, int ax) {
+  if (dim == 1) {
+    if (mid == 3) {
+      if (sol == LLF) return &launch_sweep<T, 3, SCH, LLF, 1, 0>;
+      if (sol == HLLC) return &launch_sweep<T, 3, SCH, HLLC, 1, 0>;
+    } else if (mid == 8) {
+      if (sol == LLF) return &launch_sweep<T, 8, SCH, LLF, 1, 0>;
+      if (sol == HLLC) return &launch_sweep<T, 8, SCH, HLLC, 1, 0>;
+      if (sol == HLLD) return &launch_sweep<T, 8, SCH, HLLD, 1, 0>;
+    }
+  } else if (dim == 2) {
+    if (mid == 4) {
+      if (sol == LLF) return ax == 0 ? &launch_sweep<T, 4, SCH, LLF, 2, 0> : &launch_sweep<T, 4, SCH, LLF, 2, 1>;
+      if (sol == HLLC) return ax == 0 ? &launch_sweep<T, 4, SCH, HLLC, 2, 0> : &launch_sweep<T, 4, SCH, HLLC, 2, 1>;
+    } else if (mid == 8) {
+      if (sol == LLF) return ax == 0 ? &launch_sweep<T, 8, SCH, LLF, 2, 0> : &launch_sweep<T, 8, SCH, LLF, 2, 1>;
+      if (sol == HLLC) return ax == 0 ? &launch_sweep<T, 8, SCH, HLLC, 2, 0> : &launch_sweep<T, 8, SCH, HLLC, 2, 1>;
+      if (sol == HLLD) return ax == 0 ? &launch_sweep<T, 8, SCH, HLLD, 2, 0> : &launch_sweep<T, 8, SCH, HLLD, 2, 1>;
+    }
+  }
+  return nullptr;
+}
+
+#define ASTREA_EXTERN_GET_SWEEP(T)                                               \
+  extern template SweepFn<T> get_sweep<T, PCM>(int, int, int, int);              \
+  extern template SweepFn<T> get_sweep<T, PLM>(int, int, int, int);              \
+  extern template SweepFn<T> get_sweep<T, PPM>(int, int, int, int);              \
+  extern template SweepFn<T> get_sweep<T, WENO3>(int, int, int, int);            \
+  extern template SweepFn<T> get_sweep<T, WENO5>(int, int, int, int);            \
+  extern template SweepFn<T> get_sweep<T, WENO7>(int, int, int, int);
+
+}  // namespace astrea

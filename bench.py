@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Benchmark of the per-step finite-volume update on GB300.
+
+Workload (the headline configuration): 2D Euler shear layer, gamma = 1.4,
+2048 x 2048 periodic cells on [0,1]^2, rho = 2 and v_x = +0.5 for
+|y - 0.5| < 0.25, rho = 1 and v_x = -0.5 elsewhere, p = 2.5, v_y =
+0.01 sin(4 pi x) + seeded uniform noise of amplitude 1e-3; PPM (McCorquodale-
+Colella limiter) + HLLC + SSPRK3 at CFL 0.8.  One step = one full SSPRK3 step
+(three stages) of the whole grid.  Synthetic data (seeded), no dataset.
+
+Arms:
+  default             our CUDA path; value = FP32 cell-updates/s with the state
+                      resident in HBM; also the plain FP64 rate, the FP32-vs-FP64
+                      L1(rho) error, the end-to-end rate through the C ABI with
+                      host buffers, the roofline of the sweep kernel and a CPU
+                      baseline (the oracle on a bounded sample).
+  --impl reference    the reference's algorithm on the host CPU cores (the
+                      oracle restatement, one process per core on independent
+                      bounded samples of the same workload).
+
+Multi-GPU (torchrun): independent replicas, no collective (the batched and
+single-grid workloads do not exchange data); value sums all ranks.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 20261203
+METRIC = "cell-updates/s FP32-batched vs FP64 plain (L1<=1e-5); serve p50/p99 ms"
+WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc)+HLLC+SSPRK3, CFL 0.8"
+
+
+def shear_layer(n, seed=SEED):
+    """Point primitives of the shear-layer workload, shape (n, n, 8)."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + .5) / n
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    w = np.zeros((n, n, 8))
+    inner = np.abs(Y - .5) < .25
+    w[..., 0] = np.where(inner, 2.0, 1.0)
+    w[..., 1] = np.where(inner, .5, -.5)
+    w[..., 2] = .01 * np.sin(4 * np.pi * X) + rng.uniform(-1e-3, 1e-3, size=(n, n))
+    w[..., 4] = 2.5
+    return w
+
+
+def run_config(n, precision):
+    from astrea_gb300.solver import RunConfig
+    return RunConfig(dim=2, n0=n, n1=n, model=4, precision=precision, scheme="ppm", solver="hllc",
+                     integrator="ssprk33", boundary="wrap", gamma=1.4, dx=1.0 / n, cfl=0.8, t_end=1.0)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_sample_worker(args):
+    """One bounded CPU sample: one SSPRK3 step of an n x n shear layer with the oracle."""
+    n, seed = args
+    import numpy as np_
+    sys.path.insert(0, ROOT)
+    from oracle import stepper
+    cfg = stepper.OracleConfig(dim=2, scheme="ppm", solver="hllc", integrator="ssprk33", gamma=1.4, bc="wrap",
+                               dx=1.0 / n, cfl=0.8, eig="analytic", t_end=1.0)
+    q = stepper.initialise(shear_layer(n, seed), cfg)
+    t0 = time.perf_counter()
+    with np_.errstate(all="ignore"):
+        stepper.step(q, cfg, 0.0, 1, [0, 1])
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(n=256, procs=1):
+    """Oracle (NumPy restatement of the reference) on host cores: cell-updates/s."""
+    if procs <= 1:
+        dt = cpu_sample_worker((n, SEED))
+        return n * n / dt, 1
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        t0 = time.perf_counter()
+        pool.map(cpu_sample_worker, [(n, SEED + i) for i in range(procs)])
+        wall = time.perf_counter() - t0
+    return procs * n * n / wall, procs
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, ws):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return 0
+    procs = max(1, len(os.sched_getaffinity(0)))
+    n = args.cpu_n
+    for _ in range(args.warmup):
+        cpu_sample_worker((32, SEED))
+    vals = []
+    for _ in range(args.steps):
+        v, _p = cpu_baseline(n, procs)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n * n * procs / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": f"{procs} processes x one SSPRK3 step of a {n}^2 instance"},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": procs, "kind": "port",
+                             "sample": f"{procs} independent {n}^2 instances, one step each, oracle (NumPy restatement)"},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=2048)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--cpu-n", type=int, default=192)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    from astrea_gb300 import _lib
+    from astrea_gb300.solver import Solver
+    n = args.n
+    w0 = shear_layer(n)
+
+    # ---- FP32 (headline), state resident in HBM
+    s32 = Solver(run_config(n, 32))
+    s32.initialise(w0)
+    s32.reset_clock()
+    s32.step(args.warmup, graph=True)
+    torch.cuda.synchronize()
+    barrier(ws)
+    kernel_ms = (ctypes.c_double * 3)()
+    launches = (ctypes.c_int * 3)()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as cs:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        _lib.check(s32.lib.astrea_step_timed(s32.handle, ctypes.c_void_p(s32.state.data_ptr()), args.steps,
+                                             kernel_ms, launches, ctypes.c_void_p(stream.cuda_stream)))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    barrier(ws)
+    ms = allmax(ms, ws)
+    cells = n * n
+    value = ws * cells * args.steps / (ms / 1e3)
+    clk32 = s32.clock()
+
+    # ---- roofline of the sweep kernel: algorithmic bytes per launch / mean launch time
+    C, sz = 4, 4
+    # per step: 3 stages x (first sweep: read state + write divergence = 2*C*s per cell;
+    # second sweep: stage 0 the same, stages 1-2 read state, divergence, u0 and write the result = 4*C*s)
+    alg_bytes_step = cells * C * sz * (2 + 2 + (2 + 4) + (2 + 4))
+    sweep_launches = launches[0]
+    sweep_ms = kernel_ms[0]
+    alg_per_launch = alg_bytes_step * args.steps / max(sweep_launches, 1)
+    achieved = alg_per_launch / (sweep_ms / max(sweep_launches, 1) / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    step_alg = cells * 8 * C * sz  # 8 state passes per SSPRK3 step (minimum traffic)
+
+    # ---- FP64 plain, same workload, and L1(rho) of FP32 against it after the same steps
+    s64 = Solver(run_config(n, 64))
+    s64.initialise(w0)
+    s64.reset_clock()
+    s64.step(1, graph=True)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    s64.step(args.fp64_steps, graph=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = f0.elapsed_time(f1)
+    value64 = cells * args.fp64_steps / (ms64 / 1e3)
+    # L1(rho) after the same number of steps from the same initial state
+    k = args.fp64_steps + 1
+    a32 = Solver(run_config(n, 32))
+    a32.initialise(w0)
+    a32.reset_clock()
+    a32.step(k)
+    rho32 = a32.state[0].double()
+    rho64 = s64.state[0]
+    l1 = float(torch.mean(torch.abs(rho32 - rho64)).item())
+
+    # ---- end to end through the C ABI with host buffers (pinned): H2D state, one step, D2H state
+    host = torch.empty_like(s32.state, device="cpu").pin_memory()
+    host.copy_(s32.state.cpu())
+    for _ in range(2):
+        s32.state.copy_(host, non_blocking=True)
+        s32.step(1, graph=True)
+        host.copy_(s32.state, non_blocking=True)
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(args.steps):
+        s32.state.copy_(host, non_blocking=True)
+        s32.step(1, graph=True)
+        host.copy_(s32.state, non_blocking=True)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = allmax(g0.elapsed_time(g1), ws)
+    e2e = ws * cells * args.steps / (e2e_ms / 1e3)
+    state_bytes = s32.state.numel() * s32.state.element_size()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, cores = cpu_baseline(args.cpu_n, 1)
+        cpu = {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+               "sample": f"one SSPRK3 step of a {args.cpu_n}^2 instance of the workload, oracle (NumPy), 1 core"}
+
+    if rank == 0:
+        per_step_launches = (launches[0] + launches[1] + launches[2]) / args.steps
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": cells, "precision": "fp32 (FP64 pressure recovery)",
+                       "parallelism": f"replicas x{ws}", "l2": "working set 5 x 67 MB > L2 (inputs larger than L2)"},
+            "fp64_plain": {"value": value64, "unit": "cell-updates/s", "steps": args.fp64_steps,
+                           "ms_per_step": ms64 / args.fp64_steps},
+            "fp32_over_fp64": value / ws / value64,
+            "l1_rho_fp32_vs_fp64": l1, "l1_after_steps": k,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "sweep_kernel (all sweep launches)",
+                         "peak_source": peak_kind,
+                         "step_frac": step_alg * (value / ws) / cells / 1e9 / peak},
+            "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1], "bookkeeping": kernel_ms[2]},
+            "gpu_launches": launches[0] + launches[1] + launches[2],
+            "launches_per_step": per_step_launches,
+            "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
+                    "d2h_bytes_per_step": state_bytes},
+            "clocks": cs.summary(),
+            "cpu_baseline": cpu,
+            "t_simulated": clk32["t"],
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

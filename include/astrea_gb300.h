@@ -1,0 +1,139 @@
+/*
+ * astrea_gb300.h -- C ABI of the GB300 (sm_103a) implementation of astrea's
+ * per-step finite-volume update.
+ *
+ * The reference (mervyzr/astrea) is pure Python: its "plugin API" for this
+ * path is a pair of functions selected by strings in the ``sim_variables``
+ * namedtuple,
+ *     num_methods/evolvers.py:12  evolve_space(grid, sim_variables) -> fluxes
+ *     num_methods/evolvers.py:38  evolve_time(grid, fluxes, dt, sim_variables) -> grid
+ * driven by the step loop astrea.py:31-85 (core_run).  This library is what a
+ * foreign-function binding of that path binds: plain pointers and sizes, no
+ * Python or torch types.  The Python module ``astrea_gb300.evolvers`` keeps the
+ * reference signatures on top of it (ctypes).
+ *
+ * Memory: every ``state`` argument is a caller-owned *device* buffer holding
+ * the cell-averaged conservative variables as ``nv`` component planes
+ * (structure of arrays), each plane ``n0*n1`` elements with axis 1 contiguous
+ * -- i.e. the reference's (n0, n1, 8) array with the variable axis moved first
+ * and the identically-zero variables of the chosen model left out.  Element
+ * type is double (precision 64) or float (precision 32).  ``stream`` is a
+ * cudaStream_t (NULL = legacy default stream).
+ *
+ * Errors: every int-returning function returns ASTREA_OK (0) or a negative
+ * ASTREA_ERR_* code; nothing throws across the ABI; astrea_last_error() gives
+ * a message for the calling thread.  One handle per host thread.
+ */
+#ifndef ASTREA_GB300_H
+#define ASTREA_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASTREA_OK 0
+#define ASTREA_ERR_CONFIG (-1)    /* unsupported or inconsistent configuration */
+#define ASTREA_ERR_CUDA (-2)      /* a CUDA call failed */
+#define ASTREA_ERR_OOM (-3)       /* device allocation failed / over budget */
+#define ASTREA_ERR_NONFINITE (-4) /* a non-finite wave speed or dt was produced */
+#define ASTREA_ERR_TIMEOUT (-5)   /* a bounded device wait gave up */
+#define ASTREA_ERR_ARG (-6)       /* bad pointer or size */
+
+/* enums: the reference's strings are mapped onto these by the caller
+ * (see astrea_gb300/config.py, mirroring functions/generic.py:159-286) */
+enum astrea_scheme { ASTREA_PCM = 0, ASTREA_PLM = 1, ASTREA_PPM = 2, ASTREA_WENO3 = 3, ASTREA_WENO5 = 4, ASTREA_WENO7 = 5 };
+enum astrea_solver { ASTREA_LLF = 0, ASTREA_HLLC = 1, ASTREA_HLLD = 2 };
+enum astrea_integrator { ASTREA_EULER = 0, ASTREA_SSPRK22 = 1, ASTREA_SSPRK33 = 2, ASTREA_SSPRK43 = 3 };
+enum astrea_boundary { ASTREA_EDGE = 0, ASTREA_WRAP = 1 };
+enum astrea_limiter { ASTREA_MINMOD = 0, ASTREA_SUPERBEE = 1 };
+/* stored variables: 3 = 1D Euler (rho, m_x, E); 4 = 2D Euler (rho, m_x, m_y, E);
+ * 8 = ideal MHD (rho, m_x, m_y, m_z, E, B_x, B_y, B_z) */
+
+typedef struct astrea_cfg {
+  int dim;          /* 1 or 2 (sim_variables.dimension) */
+  int n0, n1;       /* cells along axis 0 and axis 1 (n1 = 1 in 1D) */
+  int model;        /* 3, 4 or 8 */
+  int precision;    /* 64 (plain FP64) or 32 (FP32 with FP64 pressure recovery) */
+  int scheme;       /* enum astrea_scheme (sim_variables.subgrid) */
+  int solver;       /* enum astrea_solver (sim_variables.solver) */
+  int integrator;   /* enum astrea_integrator (sim_variables.timestep) */
+  int boundary;     /* enum astrea_boundary (sim_variables.boundary) */
+  int limiter;      /* PLM slope limiter, enum astrea_limiter */
+  double gamma;     /* sim_variables.gamma */
+  double dx;        /* sim_variables.dx */
+  double cfl;       /* sim_variables.cfl */
+  double t_end;     /* sim_variables.t_end */
+  int checkpoints;  /* sim_variables.checkpoints */
+} astrea_cfg;
+
+typedef struct astrea_handle astrea_handle;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int astrea_version(void);
+/* Message of the last error on this thread ("" if none). */
+const char* astrea_last_error(void);
+
+/* Create a solver for one grid (allocates its stage buffers on the current
+ * device).  Replaces building ``sim_variables`` (functions/generic.py:159-286,
+ * astrea.py:132-133). */
+int astrea_create(const astrea_cfg* cfg, astrea_handle** out);
+void astrea_destroy(astrea_handle* h);
+/* Number of stored variables (planes) and cells per plane. */
+int astrea_layout(const astrea_handle* h, int* nv, long long* cells);
+
+/* Point primitives -> cell-averaged conservatives, like
+ * constructor.initialise (functions/constructor.py:105-109).  ``prim`` and
+ * ``state_out`` use the state layout (primitive variables in ``prim``). */
+int astrea_initialise(astrea_handle* h, const void* prim, void* state_out, void* stream);
+
+/* Reset the device clock (t, next checkpoint index, axis order 0|1). */
+int astrea_reset_clock(astrea_handle* h, double t, int idx, int order, void* stream);
+
+/* Advance ``nsteps`` steps of the core_run loop body (astrea.py:66-85): the
+ * space operator, dt = cfl*min(dx/eigmax) clipped to the checkpoint, the time
+ * integrator, the axis-order flip.  dt and t stay on the device; once t
+ * reaches t_end further steps do nothing.  Asynchronous on ``stream``. */
+int astrea_step(astrea_handle* h, void* state, int nsteps, void* stream);
+
+/* Same as astrea_step, replaying one captured CUDA graph per step. */
+int astrea_graph_step(astrea_handle* h, void* state, int nsteps, void* stream);
+
+/* Same as astrea_step, with a CUDA event pair recorded on ``stream`` around
+ * every kernel launch.  kernel_ms[k] / launches[k] receive the summed device
+ * time and the launch count per kernel kind k: 0 sweep, 1 stage-0 combine,
+ * 2 dt and step bookkeeping.  Synchronises ``stream``.  (Instrumentation for
+ * measurement; no counterpart in the reference.) */
+int astrea_step_timed(astrea_handle* h, void* state, int nsteps, double* kernel_ms, int* launches, void* stream);
+
+/* Read the device clock (synchronises ``stream``).  status bit 0: a
+ * non-finite wave speed or dt was seen. */
+int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* done, int* status, void* stream);
+
+/* evolve_space (num_methods/evolvers.py:12-34): interface fluxes of every
+ * axis and the per-axis maximum wave speed.  ``order`` = 0 sweeps axis 0
+ * first (even step), 1 sweeps axis 1 first (odd step).  flux_ax0 receives
+ * (n0+1)*n1 elements per plane, flux_ax1 (n1+1)*n0 elements per plane (sweep
+ * index major, as the reference's transposed arrays); either may be NULL.
+ * eigmax (host, 2 doubles) receives eigmax of axis 0 and axis 1.
+ * Synchronises ``stream``. */
+int astrea_space(astrea_handle* h, const void* state, int order, void* flux_ax0, void* flux_ax1, double* eigmax,
+                 void* stream);
+
+/* evolve_time (num_methods/evolvers.py:38-206) with a caller-given dt: the
+ * full Runge-Kutta step, in place on ``state``.  The stage-0 fluxes are
+ * recomputed on the device from ``state`` (they are a pure function of it). */
+int astrea_time(astrea_handle* h, void* state, double dt, int order, void* stream);
+
+/* Conservative -> primitive of the whole grid (sim_variables.convert_conservative),
+ * e.g. for the per-step snapshot of astrea.py:47. */
+int astrea_to_primitive(astrea_handle* h, const void* state, void* prim_out, void* stream);
+
+/* Compensated (Neumaier, FP64) sums of every stored variable over the grid:
+ * total mass, momentum, energy (functions/analytic.py:66-79 sums them on
+ * the host).  sums_host receives nv doubles.  Synchronises ``stream``. */
+int astrea_reduce_conserved(astrea_handle* h, const void* state, double* sums_host, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ASTREA_GB300_H */

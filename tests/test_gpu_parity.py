@@ -1,0 +1,146 @@
+"""FP64 parity of the CUDA path against the oracle and the reference's golden vectors.
+
+Bars (relative to the max magnitude of the compared array):
+* against the oracle in 'analytic' wave-speed mode (the same closed form the
+  kernels evaluate): 1e-14 -- the kernels keep the reference's operation order
+  and compile FP64 without FMA, so this is bit-level agreement up to the odd
+  last-bit difference;
+* against the reference's own outputs (golden vectors, LAPACK eigenvalues):
+  1e-12, the plain-method target; WENO-7 amplifies last-bit differences of
+  dt more strongly and gets 1e-11.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from astrea_gb300 import config as C
+from astrea_gb300.solver import Solver, RunConfig, pick_model
+from oracle import stepper
+from tests import golden_io
+
+pytestmark = pytest.mark.gpu
+
+SUPPORTED_INTEGRATORS = {"euler", "ssprk22", "ssprk33", "ssprk43"}
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def oracle_cfg(meta, eig="analytic"):
+    return stepper.OracleConfig(
+        dim=meta["dim"], scheme=C.scheme_of(meta["subgrid"]), solver=C.solver_of(meta["solver"]),
+        integrator=C.integrator_of(meta["timestep"]), gamma=meta["gamma"], bc=meta["boundary"], dx=meta["dx"],
+        cfl=meta["cfl"], magnetic_2d=meta["magnetic_2d"], eig=eig, t_end=meta["t_end"])
+
+
+def gpu_cfg(meta, q0, precision=64):
+    oc = oracle_cfg(meta)
+    n = meta["cells"]
+    return RunConfig(dim=meta["dim"], n0=n, n1=n if meta["dim"] == 2 else 1,
+                     model=pick_model(meta["dim"], oc.solver, q0), precision=precision, scheme=oc.scheme,
+                     solver=oc.solver, integrator=oc.integrator, boundary=oc.bc, gamma=oc.gamma, dx=oc.dx,
+                     cfl=oc.cfl, t_end=oc.t_end)
+
+
+def runnable(name):
+    meta = golden_io.load(name)["meta"]
+    return (not meta["magnetic_2d"]) and C.integrator_of(meta["timestep"]) in SUPPORTED_INTEGRATORS
+
+
+CASES = [n for n in golden_io.case_names() if runnable(n)]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_steps_match_oracle_and_reference(name):
+    g = golden_io.load(name)
+    meta = g["meta"]
+    cfg = gpu_cfg(meta, g["q0"])
+    s = Solver(cfg)
+    s.load_conservative(g["q0"])
+    s.reset_clock(0.0, 1, 0)
+    oc = oracle_cfg(meta)
+    q_or, t, idx, order = g["q0"], 0.0, 1, stepper.initial_order(cfg.dim)
+    tol_ref = 1e-11 if oc.scheme == "weno7" else 1e-12
+    with np.errstate(all="ignore"):
+        for k in range(meta["steps"]):
+            s.step(1, graph=False)
+            q_or, t, idx, order, dt = stepper.step(q_or, oc, t, idx, order)
+            q_gpu = s.conservative().cpu().numpy()
+            clk = s.clock()
+            assert clk["dt"] == pytest.approx(dt, rel=1e-14, abs=0), (name, k)
+            assert rel_err(q_gpu, q_or) <= 1e-14, (name, k, rel_err(q_gpu, q_or))
+            assert rel_err(q_gpu, g[f"q_{k + 1}"]) <= tol_ref, (name, k, rel_err(q_gpu, g[f"q_{k + 1}"]))
+
+
+@pytest.mark.parametrize("name", [n for n in CASES if "flux_s0_p0" in golden_io.load(n)])
+def test_space_fluxes_and_eigmax(name):
+    g = golden_io.load(name)
+    meta = g["meta"]
+    cfg = gpu_cfg(meta, g["q0"])
+    s = Solver(cfg)
+    s.load_conservative(g["q0"])
+    (f0, f1), eig = s.space(order=0)
+    from astrea_gb300.solver import from_planes
+    order = stepper.initial_order(cfg.dim)
+    with np.errstate(all="ignore"):
+        fl = stepper.evolve_space(g["q0"], oracle_cfg(meta), order)
+    for pos, axis in enumerate(order):
+        F = from_planes(f0 if axis == 0 else f1, cfg.model, cfg.dim).cpu().numpy()
+        assert rel_err(F, fl[axis]["flux"]) <= 1e-14
+        assert rel_err(F, g[f"flux_s0_p{pos}"]) <= 1e-12
+        assert eig[axis] == pytest.approx(fl[axis]["eigmax"], rel=1e-15)
+        assert eig[axis] == pytest.approx(float(g[f"eigmax_s0_p{pos}"]), rel=1e-13)
+
+
+def test_initialise_matches_reference_initial_grid():
+    g = golden_io.load("sod1d_ppm_lf")
+    meta = g["meta"]
+    n = meta["cells"]
+    dx = 1.0 / n
+    x = np.linspace(-dx / 2, 1 + dx / 2, n + 2)[1:-1]
+    w = np.zeros((n, 8))
+    w[:] = [.125, 0, 0, 0, .1, 0, 0, 0]
+    w[x <= .5] = [1, 0, 0, 0, 1, 0, 0, 0]
+    s = Solver(gpu_cfg(meta, g["q0"]))
+    s.initialise(w)
+    assert np.array_equal(s.conservative().cpu().numpy(), g["q0"])
+
+
+def test_full_run_plain_config_n128_to_t_end():
+    g = golden_io.load("sod1d_plm_lf_n128", prefix="full_")
+    meta = g["meta"]
+    s = Solver(gpu_cfg(meta, g["q0"]))
+    s.load_conservative(g["q0"])
+    s.reset_clock()
+    clk = s.run()
+    assert clk["done"] and clk["t"] == g["t"] and clk["steps"] == meta["steps"]
+    assert rel_err(s.conservative().cpu().numpy(), g["qT"]) <= 1e-12
+
+
+def test_graph_replay_equals_direct_launches():
+    g = golden_io.load("khi2d_ppm_hllc")
+    meta = g["meta"]
+    a, b = Solver(gpu_cfg(meta, g["q0"])), Solver(gpu_cfg(meta, g["q0"]))
+    for s in (a, b):
+        s.load_conservative(g["q0"])
+        s.reset_clock()
+    a.step(4, graph=False)
+    b.step(4, graph=True)
+    assert torch.equal(a.state, b.state)
+    assert a.clock() == b.clock()
+
+
+def test_conservation_periodic_fp64():
+    g = golden_io.load("khi2d_plm_lf")
+    meta = g["meta"]
+    s = Solver(gpu_cfg(meta, g["q0"]))
+    s.load_conservative(g["q0"])
+    s.reset_clock()
+    before = s.conserved_sums()
+    s.step(20)
+    after = s.conserved_sums()
+    scale = np.max(np.abs(before))
+    assert np.max(np.abs(after - before)) <= 1e-12 * scale * s.state[0].numel()

@@ -31,7 +31,7 @@ class Cfg(ctypes.Structure):
         ("precision", ctypes.c_int), ("scheme", ctypes.c_int), ("solver", ctypes.c_int),
         ("integrator", ctypes.c_int), ("boundary", ctypes.c_int), ("limiter", ctypes.c_int),
         ("gamma", ctypes.c_double), ("dx", ctypes.c_double), ("cfl", ctypes.c_double), ("t_end", ctypes.c_double),
-        ("checkpoints", ctypes.c_int),
+        ("checkpoints", ctypes.c_int), ("flags", ctypes.c_int),
     ]
 
 

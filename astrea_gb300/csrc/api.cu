@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/astrea_gb300.h"
+#include "ct.cuh"
 #include "stage.cuh"
 #include "sweep_launch.cuh"
 
@@ -114,12 +115,17 @@ template <typename T> struct Engine final : IEngine {
   T* k[2] = {nullptr, nullptr};
   T* d[2] = {nullptr, nullptr};
   T* tmp = nullptr;
+  T* wf[2] = {nullptr, nullptr};  // 2D MHD: face values of each sweep
+  T* ez = nullptr;                // 2D MHD: corner electric field
   SweepFn<T> sweep[2] = {nullptr, nullptr};
 
   ~Engine() override {
-    for (int i = 0; i < 2; ++i) { cudaFree(k[i]); cudaFree(d[i]); }
+    for (int i = 0; i < 2; ++i) { cudaFree(k[i]); cudaFree(d[i]); cudaFree(wf[i]); }
     cudaFree(tmp);
+    cudaFree(ez);
   }
+
+  bool ct() const { return (cfg.flags & ASTREA_FLAG_CT) != 0; }
 
   long long plane() const { return cells; }
 
@@ -130,6 +136,13 @@ template <typename T> struct Engine final : IEngine {
       if (cudaMalloc(&d[i], bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "divergence buffer allocation failed");
     }
     if (cudaMalloc(&tmp, bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "scratch allocation failed");
+    if (ct()) {
+      const size_t b8 = sizeof(T) * 8 * (size_t)cells;
+      if (cudaMalloc(&wf[0], b8) != cudaSuccess || cudaMalloc(&wf[1], b8) != cudaSuccess ||
+          cudaMalloc(&ez, sizeof(T) * (size_t)cells) != cudaSuccess)
+        return fail(ASTREA_ERR_OOM, "constrained-transport buffer allocation failed");
+      CK(cudaFuncSetAttribute(corner_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corner_smem_bytes<T>()));
+    }
     SweepFn<T> (*getter)(int, int, int, int) = nullptr;
     switch (cfg.scheme) {
       case PCM: getter = &get_sweep<T, PCM>; break;
@@ -165,13 +178,67 @@ template <typename T> struct Engine final : IEngine {
     a.gm1 = T(cfg.gamma - 1.0);
     a.dx = cfg.dx;
     a.clock = c;
+    a.physical = (cfg.flags & ASTREA_FLAG_PHYSICAL) ? 1 : 0;
     return a;
+  }
+
+  // 2D MHD step: per stage both sweeps (storing face values), the corner
+  // field, the combine with induction rows, and the inverse reconstruction of B
+  int enqueue_step_ct(T* u, Clock* c, bool device_dt, cudaStream_t st, KTimer* tm) {
+    const int ns = stages_of(cfg.integrator);
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>((cells + threads - 1) / threads, 152LL * 16);
+    const dim3 cgrid((cfg.n0 + CTX - 1) / CTX, (cfg.n1 + CTY - 1) / CTY);
+    const dim3 rgrid((cfg.n0 + RTX - 1) / RTX, (cfg.n1 + RTY - 1) / RTY);
+    const int hll = cfg.solver != LLF;
+    for (int s = 0; s < ns; ++s) {
+      T* cur = s == 0 ? u : k[(s - 1) % 2];
+      T* out = s == ns - 1 ? u : k[s % 2];
+      SweepArgs<T> a = base_args(cur, c);
+      a.mode = 0;
+      a.want_emax = s == 0;
+      for (int ax = 0; ax < 2; ++ax) {
+        a.dout = d[ax];
+        a.wface_out = wf[ax];
+        TSTART(0);
+        CK(sweep[ax](a, st));
+        TSTOP();
+      }
+      if (s == 0 && device_dt) {
+        TSTART(2);
+        dt_kernel<<<1, 32, 0, st>>>(c, 1);
+        CK(cudaGetLastError());
+        TSTOP();
+      }
+      TSTART(1);
+      corner_kernel<T><<<cgrid, 256, corner_smem_bytes<T>(), st>>>(wf[0], wf[1], ez, cfg.n0, cfg.n1, plane(),
+                                                                   cfg.boundary, T(cfg.gamma), hll, c);
+      CK(cudaGetLastError());
+      ct_combine_kernel<T><<<blocks, threads, 0, st>>>(u, cur, d[0], d[1], ez, wf[0], wf[1], tmp, cfg.n0, cfg.n1,
+                                                       plane(), cfg.boundary, cfg.dx, cfg.integrator, s, c);
+      CK(cudaGetLastError());
+      refine_kernel<T, 0><<<rgrid, 256, 0, st>>>(tmp, out, cfg.n0, cfg.n1, plane(), cfg.boundary, c);
+      CK(cudaGetLastError());
+      refine_kernel<T, 1><<<rgrid, 256, 0, st>>>(tmp, out, cfg.n0, cfg.n1, plane(), cfg.boundary, c);
+      CK(cudaGetLastError());
+      copy_nonB_kernel<T><<<blocks, threads, 0, st>>>(tmp, out, plane(), cells, c);
+      CK(cudaGetLastError());
+      TSTOP();
+    }
+    if (device_dt) {
+      TSTART(2);
+      end_step_kernel<<<1, 32, 0, st>>>(c, 1);
+      CK(cudaGetLastError());
+      TSTOP();
+    }
+    return ASTREA_OK;
   }
 
   int enqueue_step(void* state, Clock* c, bool device_dt, cudaStream_t st, KTimer* tm = nullptr) override {
     T* u = static_cast<T*>(state);
     const int ns = stages_of(cfg.integrator);
     if (ns < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this build");
+    if (ct()) return enqueue_step_ct(u, c, device_dt, st, tm);
     const long long n = cells;
     const int threads = 256;
     const int blocks = (int)std::min<long long>((n + threads - 1) / threads, 152LL * 16);
@@ -322,6 +389,8 @@ static int validate(const astrea_cfg* c) {
   if (c->solver < 0 || c->solver > HLLD) return fail(ASTREA_ERR_CONFIG, "unknown solver");
   if (stages_of(c->integrator) < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this build");
   if (c->boundary != EDGE && c->boundary != WRAP) return fail(ASTREA_ERR_CONFIG, "boundary must be edge(0) or wrap(1)");
+  if ((c->flags & ASTREA_FLAG_CT) && (c->dim != 2 || c->model != 8))
+    return fail(ASTREA_ERR_CONFIG, "constrained transport needs dim 2 and model 8");
   if (!(c->dx > 0) || !(c->cfl > 0) || !(c->gamma > 1) || c->checkpoints < 1)
     return fail(ASTREA_ERR_CONFIG, "dx, cfl > 0, gamma > 1, checkpoints >= 1 required");
   if ((long long)c->n0 * (long long)(c->dim == 2 ? c->n1 : 1) > (1LL << 31))

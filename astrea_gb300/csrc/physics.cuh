@@ -191,9 +191,11 @@ __device__ __forceinline__ void llf(T alpha, const T* qp, const T* qm, const T* 
 // HLLC (solvers.py:92-138).  ``label`` is the sweep's iteration position: the
 // normal velocity is component label+1 while the star normal momentum is
 // always written to component 1; with no wave condition met the flux is f_plus.
+// ``physical`` (not a reference option): star normal momentum in component
+// label+1 and f_minus where sL > 0 (the textbook solver).
 template <class M, typename T>
-__device__ __forceinline__ void hllc(int label, T gamma, const T* wp, const T* wm, const T* qp, const T* qm,
-                                     const T* fp, const T* fm, T* F) {
+__device__ __forceinline__ void hllc(int label, int physical, T gamma, const T* wp, const T* wm, const T* qp,
+                                     const T* qm, const T* fp, const T* fm, T* F) {
   const T rL = wm[0], pL = wm[4], rR = wp[0], pR = wp[4];
   T uL, uR;
   if constexpr (M::VY) { uL = label == 0 ? wm[1] : wm[2]; uR = label == 0 ? wp[1] : wp[2]; }
@@ -211,8 +213,9 @@ __device__ __forceinline__ void hllc(int label, T gamma, const T* wp, const T* w
   const bool m2 = (sM <= T(0)) && (T(0) <= sR);
   const bool m1 = (sL <= T(0)) && (T(0) < sM);
   if (m3 || !(m1 || m2)) {
+    const T* f0 = (!m3 && physical) ? fm : fp;
 #pragma unroll
-    for (int s = 0; s < M::NV; ++s) F[M::var(s)] = fp[M::var(s)];
+    for (int s = 0; s < M::NV; ++s) F[M::var(s)] = f0[M::var(s)];
     return;
   }
   // star state of the side that is selected (m2 has priority over m1)
@@ -226,7 +229,9 @@ __device__ __forceinline__ void hllc(int label, T gamma, const T* wp, const T* w
   T Qs[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) Qs[k] = Q[k] * coeff;
-  Qs[1] = (rho * coeff) * sM;
+  const T mstar = (rho * coeff) * sM;
+  if (physical && label == 1) Qs[2] = mstar;
+  else Qs[1] = mstar;
   Qs[4] = Qs[4] + (coeff * (sM - u)) * (rho * sM + dvd(p, s - u));
 #pragma unroll
   for (int k = 0; k < M::NV; ++k) {
@@ -236,12 +241,12 @@ __device__ __forceinline__ void hllc(int label, T gamma, const T* wp, const T* w
 }
 
 // HLLD fast speed: the 'normal' field is always B_x (solvers.py:144-153)
-template <typename T> __device__ __forceinline__ T hlld_fast(const T* w, T gamma) {
+template <typename T> __device__ __forceinline__ T hlld_fast(const T* w, T gamma, int nb) {
   const T rho = w[0];
   const T cs = sqrt_(dvd(gamma * w[4], rho));
   const T sr = sqrt_(rho);
   const T ca = dvd(norm3(w[5], w[6], w[7]), sr);
-  const T cax = dvd(w[5], sr);
+  const T cax = dvd(nb == 0 ? w[5] : (nb == 1 ? w[6] : w[7]), sr);
   const T cs2 = cs * cs, ca2 = ca * ca;
   return sqrt_(T(.5) * ((cs2 + ca2) + sqrt_(((cs2 + ca2) * (cs2 + ca2)) - ((T(4) * cs2) * (cax * cax)))));
 }
@@ -251,13 +256,14 @@ template <typename T> __device__ __forceinline__ T pick3(T x0, T x1, T x2, int i
 // HLLD of Miyoshi & Kusano (solvers.py:142-232), reference quirks kept.  Bn is
 // component label+5 of the cell-averaged state right of the interface.
 template <typename T>
-__device__ void hlld(int label, T gamma, const T* wSr, const T* wp, const T* wm, const T* qp, const T* qm,
-                     const T* fp, const T* fm, T* F) {
+__device__ void hlld(int label, int physical, T gamma, const T* wSr, const T* wp, const T* wm, const T* qp,
+                     const T* qm, const T* fp, const T* fm, T* F) {
   const int a = label, o = label + 1, p = (label + 2) % 3;
   const T rL = wm[0], pL = wm[4], rR = wp[0], pR = wp[4];
   const T uL = pick3(wm[1], wm[2], wm[3], a), uR = pick3(wp[1], wp[2], wp[3], a);
   const T Bn = pick3(wSr[5], wSr[6], wSr[7], a);
-  const T cfL = hlld_fast(wm, gamma), cfR = hlld_fast(wp, gamma);
+  const int nb = physical ? label : 0;
+  const T cfL = hlld_fast(wm, gamma, nb), cfR = hlld_fast(wp, gamma, nb);
   const T umin = npmin(uL, uR), cmax = npmax(cfL, cfR);
   const T sL = umin - cmax, sR = umin + cmax;
   const T nBL = nsq3(wm[5], wm[6], wm[7]), nBR = nsq3(wp[5], wp[6], wp[7]);

@@ -35,6 +35,7 @@ template <typename T> struct SweepArgs {
   int mode;           // 0: store divergence, 1: add other divergence + combine, 2: combine (sole sweep)
   int integ, stage;   // Runge-Kutta scheme and stage for the combine
   int want_emax;      // accumulate the max wave speed of this axis into the clock
+  int physical;       // textbook HLLC/HLLD (label = physical axis) instead of the reference's
   T gamma, gm1;
   double dx;
   T* dout;            // mode 0: divergence output (NV planes)
@@ -43,6 +44,7 @@ template <typename T> struct SweepArgs {
   T* out;             // combine output
   Clock* clock;
   T* flux_out;        // optional: interface fluxes [NV][Ns+1][Nt]
+  T* wface_out;       // optional (2D MHD): face value at i+1/2 of every cell, physical layout [8][n0][n1]
 };
 
 template <int SCH, int DIM, int TS, int TT> struct Geom {
@@ -153,7 +155,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
   const T gamma = a.gamma, gm1 = a.gm1;
   const int tid = threadIdx.x, nth = blockDim.x;
   // axis label of this sweep: its position in the step's iteration order
-  const int label = a.label >= 0 ? a.label : (DIM == 1 ? 0 : (AX == 0 ? a.clock->order : 1 - a.clock->order));
+  const int label = a.physical ? (DIM == 1 ? 0 : AX)
+                  : (a.label >= 0 ? a.label : (DIM == 1 ? 0 : (AX == 0 ? a.clock->order : 1 - a.clock->order)));
 
   auto gidx = [&](int gs, int gt) -> long long {
     if (DIM == 1) return gs;
@@ -249,6 +252,14 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
       reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr);
       s_R[((0 * NV + s) * H + row) * W + col] = wl;
       s_R[((1 * NV + s) * H + row) * W + col] = wr;
+      if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) {
+        // the face value the constrained transport uses: PPM's unlimited 4th-order
+        // face (ppm.py:38-42), the right face value of the other schemes (weno.py:168, plm.py:39)
+        T fv;
+        if constexpr (SCH == PPM) fv = ppm_face<T>(at, rs_, rs);
+        else fv = wr;
+        a.wface_out[M::var(s) * a.plane + gidx(vs, vt)] = fv;
+      }
     }
   }
   __syncthreads();
@@ -294,9 +305,9 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
       const T alpha = npmax(s_lam[lam_row * G::YW + k_local], s_lam[lam_row * G::YW + k_local + 1]);
       llf<M>(alpha, qp, qm, fp, fm, F);
     } else if constexpr (SOL == HLLC) {
-      hllc<M>(label, gamma, wp, wm, qp, qm, fp, fm, F);
+      hllc<M>(label, a.physical, gamma, wp, wm, qp, qm, fp, fm, F);
     } else {
-      hlld<T>(label, gamma, wSr, wp, wm, qp, qm, fp, fm, F);
+      hlld<T>(label, a.physical, gamma, wSr, wp, wm, qp, qm, fp, fm, F);
     }
   };
   auto load_wS = [&](int x, int rt, T* out) {

@@ -39,6 +39,8 @@ class RunConfig:
     cfl: float = 0.8
     t_end: float = 0.2
     checkpoints: int = 1
+    compat: bool = True  # False: textbook HLLC/HLLD (not a reference option)
+    magnetic_2d: bool = False  # constrained-transport 2D MHD (sim_variables.magnetic_2d)
 
     def to_c(self):
         if self.solver not in C.SOLVER or self.solver == "lw":
@@ -49,7 +51,8 @@ class RunConfig:
                         precision=self.precision, scheme=C.SCHEME[self.scheme], solver=C.SOLVER[self.solver],
                         integrator=C.INTEGRATOR[self.integrator], boundary=C.BOUNDARY[self.boundary],
                         limiter=C.LIMITER[self.limiter], gamma=float(self.gamma), dx=float(self.dx),
-                        cfl=float(self.cfl), t_end=float(self.t_end), checkpoints=int(self.checkpoints))
+                        cfl=float(self.cfl), t_end=float(self.t_end), checkpoints=int(self.checkpoints),
+                        flags=(0 if self.compat else 1) | (2 if self.magnetic_2d else 0))
 
     @property
     def shape(self):
@@ -79,15 +82,14 @@ def config_from_sim_variables(sv, precision=64, model=None, grid=None):
     scheme = C.scheme_of(sv.subgrid)
     solver = C.solver_of(sv.solver, getattr(sv, "solver_category", None))
     integrator = C.integrator_of(sv.timestep)
-    if getattr(sv, "magnetic_2d", False):
-        raise C.ConfigError("2D constrained-transport MHD is not provided by the CUDA library yet")
+    magnetic_2d = bool(getattr(sv, "magnetic_2d", False))
     n = int(sv.cells)
     if model is None:
-        model = pick_model(dim, solver, grid)
+        model = 8 if magnetic_2d else pick_model(dim, solver, grid)
     return RunConfig(dim=dim, n0=n, n1=n if dim == 2 else 1, model=model, precision=precision, scheme=scheme,
                      solver=solver, integrator=integrator, boundary=sv.boundary, gamma=float(sv.gamma),
                      dx=float(sv.dx), cfl=float(sv.cfl), t_end=float(sv.t_end),
-                     checkpoints=int(getattr(sv, "checkpoints", 1)))
+                     checkpoints=int(getattr(sv, "checkpoints", 1)), magnetic_2d=magnetic_2d)
 
 
 def to_planes(grid, model, dtype, device):

@@ -64,7 +64,18 @@ typedef struct astrea_cfg {
   double cfl;       /* sim_variables.cfl */
   double t_end;     /* sim_variables.t_end */
   int checkpoints;  /* sim_variables.checkpoints */
+  int flags;        /* ASTREA_FLAG_* */
 } astrea_cfg;
+
+/* flags: ASTREA_FLAG_PHYSICAL selects textbook HLLC/HLLD in place of the
+ * reference's (whose 2D sweeps pick the normal velocity by iteration position,
+ * write the star normal momentum to component 1 and take f_plus when sL > 0,
+ * num_methods/solvers.py:34-36,104-137).  Not a reference option. */
+#define ASTREA_FLAG_PHYSICAL 1
+/* ASTREA_FLAG_CT: 2D MHD with the reference's fourth-order upwind constrained
+ * transport (sim_variables.magnetic_2d; num_methods/mag_field.py).  Requires
+ * dim 2 and model 8. */
+#define ASTREA_FLAG_CT 2
 
 typedef struct astrea_handle astrea_handle;
 

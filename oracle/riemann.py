@@ -26,12 +26,16 @@ def lax_wendroff(char_speed2_over_max, q_plus, q_minus, f_plus, f_minus):
     return .5 * (f_minus + f_plus) - .5 * ((q_plus - q_minus) * char_speed2_over_max[..., None])
 
 
-def hllc(label, gamma, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus):
+def hllc(label, gamma, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus, physical=False):
     """HLLC (solvers.py:92-138) with the reference's quirks kept.
 
     * The normal velocity is component ``label+1``.
     * The star-state normal momentum is always written to component 1.
     * Where no wave condition holds (sL > 0) the flux is ``f_plus``.
+
+    ``physical=True`` (not in the reference) is the textbook solver: ``label``
+    is then the physical sweep axis, the star normal momentum goes to
+    component ``label+1`` and the sL > 0 flux is ``f_minus``.
     """
     rL, uL, pL, QL = w_minus[..., 0], w_minus[..., label + 1], w_minus[..., 4], q_minus
     rR, uR, pR, QR = w_plus[..., 0], w_plus[..., label + 1], w_plus[..., 4], q_plus
@@ -47,16 +51,18 @@ def hllc(label, gamma, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus):
     sR = np.maximum(uR + cR, u_hat + c_hat)
     sM = divide(pR - pL + rL * uL * (sL - uL) - rR * uR * (sR - uR), rL * (sL - uL) - rR * (sR - uR))
 
+    mom = label + 1 if physical else 1
+
     def star(rho, u, p, Q, s):
         coeff = divide(s - u, s - sM)
         Qs = Q * coeff[..., None]
-        Qs[..., 1] = rho * coeff * sM
+        Qs[..., mom] = rho * coeff * sM
         Qs[..., 4] = Qs[..., 4] + coeff * (sM - u) * (rho * sM + divide(p, s - u))
         return Qs
 
     QLs = star(rL, uL, pL, QL, sL)
     QRs = star(rR, uR, pR, QR, sR)
-    F = np.copy(f_plus)
+    F = np.copy(f_minus if physical else f_plus)
     fLs = f_minus + (QLs - QL) * sL[..., None]
     fRs = f_plus + (QRs - QR) * sR[..., None]
     m = (sL <= 0) & (0 < sM)
@@ -68,22 +74,24 @@ def hllc(label, gamma, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus):
     return F
 
 
-def _fast_speed_bx(w, gamma):
+def _fast_speed_bx(w, gamma, normal=0):
     """HLLD's fast speed; the 'normal' field is always B_x (solvers.py:144-153)."""
     rho, P, B = w[..., 0], w[..., 4], w[..., 5:8]
     with np.errstate(invalid="ignore"):
         cs = np.sqrt(divide(gamma * P, rho))
         ca = divide(norm3(B), np.sqrt(rho))
-        cax = divide(B[..., 0], np.sqrt(rho))
+        cax = divide(B[..., normal], np.sqrt(rho))
         return np.sqrt(.5 * (cs ** 2 + ca ** 2 + np.sqrt(((cs ** 2 + ca ** 2) ** 2) - (4 * (cs ** 2) * (cax ** 2)))))
 
 
-def hlld(label, gamma, wS_right, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus):
+def hlld(label, gamma, wS_right, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus, physical=False):
     """HLLD of Miyoshi & Kusano (solvers.py:142-232), reference quirks kept.
 
     ``wS_right`` is the cell-averaged primitive of the cell right of each
     interface (``add_boundary(wS)[1:]``, solvers.py:168); its component
     ``label+5`` is the normal field used in the star and double-star states.
+    ``physical=True`` (not in the reference): ``label`` is the physical sweep
+    axis and the fast speed uses the normal field B[label].
     """
     a, o, p = label % 3, (label + 1) % 3, (label + 2) % 3
     rL, vL, pL, BL, QL = w_minus[..., 0], w_minus[..., 1:4], w_minus[..., 4], w_minus[..., 5:8], q_minus
@@ -91,7 +99,8 @@ def hlld(label, gamma, wS_right, w_plus, w_minus, q_plus, q_minus, f_plus, f_min
     Bn = wS_right[..., a + 5]
     uL, uR = vL[..., label], vR[..., label]
 
-    cfL, cfR = _fast_speed_bx(w_minus, gamma), _fast_speed_bx(w_plus, gamma)
+    nb = label if physical else 0
+    cfL, cfR = _fast_speed_bx(w_minus, gamma, nb), _fast_speed_bx(w_plus, gamma, nb)
     sL = np.minimum(uL, uR) - np.maximum(cfL, cfR)
     sR = np.minimum(uL, uR) + np.maximum(cfL, cfR)
     sM = divide(pR - pL + rL * uL * (sL - uL) - rR * uR * (sR - uR) + .5 * (nsq(BR)) - .5 * (nsq(BL)),

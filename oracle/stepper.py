@@ -34,6 +34,7 @@ class OracleConfig:
     magnetic_2d: bool = False
     limiter: str = "minmod"      # PLM slope limiter: minmod | superbee
     eig: str = "lapack"          # lapack (as the reference) | analytic (as the kernels)
+    compat: bool = True          # reference quirks in HLLC/HLLD (False: physical-axis solvers, not in the reference)
     flatten: bool = False        # PPM flattening (parity unpinned)
     viscosity: bool = False      # PPM artificial viscosity (parity unpinned)
     av_alpha: float = .3
@@ -138,13 +139,16 @@ def sweep(grid, cfg, axis, label):
     eigmax = np.max(alpha)
     wS_right = fv.gather_range(wS, 0, n + 1, bc)
 
+    phys = not cfg.compat
+    lab = axis if phys else label
+
     def solve(wp_, wm_, qp_, qm_, fp_, fm_):
         if cfg.solver == "llf":
             return riemann.llf(alpha, qp_, qm_, fp_, fm_)
         if cfg.solver == "hllc":
-            return riemann.hllc(label, g, wp_, wm_, qp_, qm_, fp_, fm_)
+            return riemann.hllc(lab, g, wp_, wm_, qp_, qm_, fp_, fm_, physical=phys)
         if cfg.solver == "hlld":
-            return riemann.hlld(label, g, wS_right, wp_, wm_, qp_, qm_, fp_, fm_)
+            return riemann.hlld(lab, g, wS_right, wp_, wm_, qp_, qm_, fp_, fm_, physical=phys)
         raise ValueError(cfg.solver)
 
     F_avg = solve(wp, wm, qp, qm, fp, fm)

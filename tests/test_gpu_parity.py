@@ -29,25 +29,25 @@ def rel_err(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
-def oracle_cfg(meta, eig="analytic"):
+def oracle_cfg(meta, eig="analytic", compat=True):
     return stepper.OracleConfig(
         dim=meta["dim"], scheme=C.scheme_of(meta["subgrid"]), solver=C.solver_of(meta["solver"]),
         integrator=C.integrator_of(meta["timestep"]), gamma=meta["gamma"], bc=meta["boundary"], dx=meta["dx"],
-        cfl=meta["cfl"], magnetic_2d=meta["magnetic_2d"], eig=eig, t_end=meta["t_end"])
+        cfl=meta["cfl"], magnetic_2d=meta["magnetic_2d"], eig=eig, t_end=meta["t_end"], compat=compat)
 
 
-def gpu_cfg(meta, q0, precision=64):
+def gpu_cfg(meta, q0, precision=64, compat=True):
     oc = oracle_cfg(meta)
     n = meta["cells"]
-    return RunConfig(dim=meta["dim"], n0=n, n1=n if meta["dim"] == 2 else 1,
-                     model=pick_model(meta["dim"], oc.solver, q0), precision=precision, scheme=oc.scheme,
-                     solver=oc.solver, integrator=oc.integrator, boundary=oc.bc, gamma=oc.gamma, dx=oc.dx,
-                     cfl=oc.cfl, t_end=oc.t_end)
+    model = 8 if meta["magnetic_2d"] else pick_model(meta["dim"], oc.solver, q0)
+    return RunConfig(dim=meta["dim"], n0=n, n1=n if meta["dim"] == 2 else 1, model=model, precision=precision,
+                     scheme=oc.scheme, solver=oc.solver, integrator=oc.integrator, boundary=oc.bc, gamma=oc.gamma,
+                     dx=oc.dx, cfl=oc.cfl, t_end=oc.t_end, compat=compat, magnetic_2d=meta["magnetic_2d"])
 
 
 def runnable(name):
     meta = golden_io.load(name)["meta"]
-    return (not meta["magnetic_2d"]) and C.integrator_of(meta["timestep"]) in SUPPORTED_INTEGRATORS
+    return C.integrator_of(meta["timestep"]) in SUPPORTED_INTEGRATORS
 
 
 CASES = [n for n in golden_io.case_names() if runnable(n)]
@@ -133,14 +133,79 @@ def test_graph_replay_equals_direct_launches():
     assert a.clock() == b.clock()
 
 
+def shear_layer(n, seed=7):
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + .5) / n
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    w = np.zeros((n, n, 8))
+    inner = np.abs(Y - .5) < .25
+    w[..., 0] = np.where(inner, 2.0, 1.0)
+    w[..., 1] = np.where(inner, .5, -.5)
+    w[..., 2] = .01 * np.sin(4 * np.pi * X) + rng.uniform(-1e-3, 1e-3, size=(n, n))
+    w[..., 4] = 2.5
+    return w
+
+
+def shear_cfg(n, precision=64, scheme="ppm", solver="hllc", compat=False):
+    return RunConfig(dim=2, n0=n, n1=n, model=4, precision=precision, scheme=scheme, solver=solver,
+                     integrator="ssprk33", boundary="wrap", gamma=1.4, dx=1.0 / n, cfl=0.8, t_end=1.0, compat=compat)
+
+
 def test_conservation_periodic_fp64():
-    g = golden_io.load("khi2d_plm_lf")
-    meta = g["meta"]
-    s = Solver(gpu_cfg(meta, g["q0"]))
-    s.load_conservative(g["q0"])
+    # the reference's own 2D HLLC loses positivity on this flow within a few steps,
+    # so conservation is checked with the textbook solver (same flux-difference form)
+    s = Solver(shear_cfg(48))
+    s.initialise(shear_layer(48))
     s.reset_clock()
     before = s.conserved_sums()
     s.step(20)
     after = s.conserved_sums()
-    scale = np.max(np.abs(before))
-    assert np.max(np.abs(after - before)) <= 1e-12 * scale * s.state[0].numel()
+    assert s.clock()["status"] == 0
+    assert np.max(np.abs(after - before) / np.abs(before).max()) <= 1e-13
+
+
+@pytest.mark.parametrize("scheme,solver", [("ppm", "hllc"), ("plm", "hllc"), ("weno5", "hllc"), ("ppm", "llf")])
+def test_physical_mode_matches_oracle(scheme, solver):
+    n = 32
+    w = shear_layer(n)
+    s = Solver(shear_cfg(n, scheme=scheme, solver=solver))
+    s.initialise(w)
+    s.reset_clock()
+    oc = stepper.OracleConfig(dim=2, scheme=scheme, solver=solver, integrator="ssprk33", gamma=1.4, bc="wrap",
+                              dx=1.0 / n, cfl=0.8, eig="analytic", t_end=1.0, compat=False)
+    q = stepper.initialise(w, oc)
+    t, idx, order = 0.0, 1, [0, 1]
+    with np.errstate(all="ignore"):
+        for k in range(4):
+            q, t, idx, order, dt = stepper.step(q, oc, t, idx, order)
+    s.step(4)
+    assert rel_err(s.conservative().cpu().numpy(), q) <= 1e-14
+
+
+def test_physical_mode_hlld_1d_matches_oracle():
+    g = golden_io.load("bw1d_plm_hlld")
+    meta = g["meta"]
+    s = Solver(gpu_cfg(meta, g["q0"], compat=False))
+    s.load_conservative(g["q0"])
+    s.reset_clock()
+    oc = oracle_cfg(meta, compat=False)
+    q, t, idx, order = g["q0"], 0.0, 1, [0]
+    with np.errstate(all="ignore"):
+        for k in range(3):
+            q, t, idx, order, dt = stepper.step(q, oc, t, idx, order)
+    s.step(3)
+    assert rel_err(s.conservative().cpu().numpy(), q) <= 1e-14
+
+
+def test_fp32_against_fp64_shear_layer():
+    # FP32 bulk arithmetic (FP64 pressure recovery): L1(rho) against the FP64 run after 10 steps
+    n = 64
+    w = shear_layer(n)
+    a, b = Solver(shear_cfg(n, 64)), Solver(shear_cfg(n, 32))
+    for s in (a, b):
+        s.initialise(w)
+        s.reset_clock()
+        s.step(10)
+    l1 = float(torch.mean(torch.abs(b.state[0].double() - a.state[0])).item())
+    assert l1 <= 1e-5, l1
+    assert abs(a.clock()["t"] - b.clock()["t"]) <= 1e-5 * a.clock()["t"]

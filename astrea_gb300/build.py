@@ -39,7 +39,7 @@ def sources():
 
 
 def flags_for(name):
-    if name.startswith("sweep_f32"):
+    if name.startswith(("sweep_f32", "batch_k_f32")):
         return ["--fmad=true"]
     return ["--fmad=false"]
 

@@ -28,20 +28,9 @@ ASTREA_EXTERN_GET_SWEEP(float)
 
 using namespace astrea;
 
-static thread_local std::string g_last_error;
+#include "host_common.h"
 
-static int fail(int code, const std::string& msg) {
-  g_last_error = msg;
-  return code;
-}
-static int cuda_fail(cudaError_t e, const char* where) {
-  return fail(ASTREA_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
-}
-#define CK(call)                                        \
-  do {                                                  \
-    cudaError_t e_ = (call);                            \
-    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
-  } while (0)
+thread_local std::string g_last_error;
 
 static int stages_of(int integ) {
   switch (integ) {

@@ -1,0 +1,371 @@
+// C ABI of the batched engine (astrea_batch_*): many independent grids in
+// one state arena, advanced together with persistent sweep kernels.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "batch_launch.cuh"
+#include "host_common.h"
+
+using namespace astrea;
+
+namespace astrea {
+ASTREA_EXTERN_BATCH(float, 1)
+ASTREA_EXTERN_BATCH(float, 2)
+ASTREA_EXTERN_BATCH(double, 1)
+ASTREA_EXTERN_BATCH(double, 2)
+}  // namespace astrea
+
+template <typename T> static BatchFn<T> batched_for(int model, int dim, int ax) {
+  return dim == 1 ? get_batched<T, 1>(model, ax) : get_batched<T, 2>(model, ax);
+}
+template <typename T> static int occupancy_for(int model, int dim, int ax) {
+  return dim == 1 ? get_occupancy<T, 1>(model, ax) : get_occupancy<T, 2>(model, ax);
+}
+
+namespace {
+
+int combo_of(int scheme, int solver, int model, int* out) {
+  const bool hll = solver != LLF;
+  if (hll && solver != (model == 8 ? HLLD : HLLC)) return -1;
+  switch (scheme) {
+    case PLM: *out = hll ? C_PLM_HLL : C_PLM_LLF; return 0;
+    case PPM: *out = hll ? C_PPM_HLL : C_PPM_LLF; return 0;
+    case WENO5: *out = hll ? C_WENO5_HLL : C_WENO5_LLF; return 0;
+    default: return -1;
+  }
+}
+
+}  // namespace
+
+struct IBatch {
+  int dim = 2, model = 4, precision = 32, integrator = SSPRK33, ngrids = 0, nv = 0;
+  std::vector<astrea_grid> host_grids;
+  std::vector<long long> cum;  // cell offsets, ngrids + 1
+  long long total_cells = 0;
+  Clock* clocks = nullptr;
+  long long* d_cum = nullptr;
+  int* counters = nullptr;  // one work counter per sweep launch of a step
+  BItem* items[2] = {nullptr, nullptr};
+  int nitems[2] = {0, 0};
+  cudaGraphExec_t graph = nullptr;
+  void* graph_arena = nullptr;
+  virtual ~IBatch() {
+    if (graph) cudaGraphExecDestroy(graph);
+    cudaFree(clocks);
+    cudaFree(d_cum);
+    cudaFree(counters);
+    cudaFree(items[0]);
+    cudaFree(items[1]);
+  }
+  virtual int alloc() = 0;
+  virtual int enqueue_step(void* arena, cudaStream_t st) = 0;
+  virtual int initialise(const void* prim, void* arena, cudaStream_t st) = 0;
+};
+
+struct astrea_batch {
+  IBatch* b;
+};
+
+static int stages_count(int integ) {
+  switch (integ) {
+    case EULER: return 1;
+    case SSPRK22: return 2;
+    case SSPRK33: return 3;
+    case SSPRK43: return 4;
+    default: return -1;
+  }
+}
+
+template <typename T> struct Batch final : IBatch {
+  T* k0 = nullptr;
+  T* k1 = nullptr;
+  T* d0 = nullptr;
+  T* d1 = nullptr;
+  T* tmp = nullptr;
+  BGrid<T>* d_grids = nullptr;
+  BatchFn<T> sweep[2] = {nullptr, nullptr};
+  int nctas[2] = {0, 0};
+
+  ~Batch() override {
+    cudaFree(k0); cudaFree(k1); cudaFree(d0); cudaFree(d1); cudaFree(tmp); cudaFree(d_grids);
+  }
+
+  int alloc() override {
+    const size_t bytes = sizeof(T) * (size_t)nv * (size_t)total_cells;
+    if (cudaMalloc(&k0, bytes) != cudaSuccess || cudaMalloc(&k1, bytes) != cudaSuccess ||
+        cudaMalloc(&d0, bytes) != cudaSuccess || cudaMalloc(&d1, bytes) != cudaSuccess ||
+        cudaMalloc(&tmp, bytes) != cudaSuccess)
+      return fail(ASTREA_ERR_OOM, "batch stage buffers allocation failed");
+    std::vector<BGrid<T>> hg(ngrids);
+    for (int g = 0; g < ngrids; ++g) {
+      const astrea_grid& a = host_grids[g];
+      BGrid<T>& d = hg[g];
+      d.base = (long long)nv * cum[g];
+      d.cells = cum[g + 1] - cum[g];
+      d.n0 = a.n0;
+      d.n1 = dim == 1 ? 1 : a.n1;
+      d.bc = a.boundary;
+      d.limiter = a.limiter;
+      d.physical = (a.flags & ASTREA_FLAG_PHYSICAL) ? 1 : 0;
+      if (combo_of(a.scheme, a.solver, model, &d.combo)) return fail(ASTREA_ERR_CONFIG, "batch grid has an unsupported scheme/solver");
+      d.gamma = T(a.gamma);
+      d.gm1 = T(a.gamma - 1.0);
+      d.dx = a.dx;
+    }
+    CK(cudaMalloc(&d_grids, sizeof(BGrid<T>) * ngrids));
+    CK(cudaMemcpy(d_grids, hg.data(), sizeof(BGrid<T>) * ngrids, cudaMemcpyHostToDevice));
+    // work lists, largest grids first
+    std::vector<int> order(ngrids);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cum[x + 1] - cum[x] > cum[y + 1] - cum[y]; });
+    int dev_sms = 0, dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev));
+    for (int ax = 0; ax < dim; ++ax) {
+      const int TS = dim == 1 ? BTS1 : BTS2, TT = dim == 1 ? 1 : BTT2;
+      std::vector<BItem> it;
+      for (int g : order) {
+        const astrea_grid& a = host_grids[g];
+        const int Ns = dim == 1 ? a.n0 : (ax == 0 ? a.n0 : a.n1);
+        const int Nt = dim == 1 ? 1 : (ax == 0 ? a.n1 : a.n0);
+        for (int s0 = 0; s0 < Ns; s0 += TS)
+          for (int t0 = 0; t0 < Nt; t0 += TT) it.push_back(BItem{g, s0, t0});
+      }
+      nitems[ax] = (int)it.size();
+      CK(cudaMalloc(&items[ax], sizeof(BItem) * it.size()));
+      CK(cudaMemcpy(items[ax], it.data(), sizeof(BItem) * it.size(), cudaMemcpyHostToDevice));
+      sweep[ax] = batched_for<T>(model, dim, ax);
+      if (!sweep[ax]) return fail(ASTREA_ERR_CONFIG, "no batched kernel for this model/dimension");
+      BatchArgs<T> probe{};
+      CK(sweep[ax](probe, 0, nullptr));
+      const int occ = std::max(1, occupancy_for<T>(model, dim, ax));
+      nctas[ax] = std::max(1, std::min(nitems[ax], occ * dev_sms));
+    }
+    CK(cudaMalloc(&counters, sizeof(int) * 16));
+    return ASTREA_OK;
+  }
+
+  BatchArgs<T> args(T* u) const {
+    BatchArgs<T> b{};
+    b.grids = d_grids;
+    b.clocks = clocks;
+    b.u = u;
+    b.k0 = k0;
+    b.k1 = k1;
+    b.d0 = d0;
+    b.d1 = d1;
+    b.integ = integrator;
+    return b;
+  }
+
+  int launch_sweep(BatchArgs<T> b, int ax, int slot, cudaStream_t st) {
+    b.items = items[ax];
+    b.nitems = nitems[ax];
+    b.counter = counters + slot;
+    CK(cudaMemsetAsync(counters + slot, 0, sizeof(int), st));
+    CK(sweep[ax](b, nctas[ax], st));
+    return ASTREA_OK;
+  }
+
+  int enqueue_step(void* arena, cudaStream_t st) override {
+    T* u = static_cast<T*>(arena);
+    const int ns = stages_count(integrator);
+    int slot = 0;
+    BatchArgs<T> b = args(u);
+    // stage 0
+    b.stage = 0;
+    b.mode = 0;
+    b.want_emax = 1;
+    for (int ax = 0; ax < dim; ++ax) {
+      b.dout_sel = ax;
+      int rc = launch_sweep(b, ax, slot++, st);
+      if (rc) return rc;
+    }
+    dt_kernel<<<(ngrids + 127) / 128, 128, 0, st>>>(clocks, ngrids);
+    CK(cudaGetLastError());
+    {
+      const int threads = 256;
+      const int blocks = (int)std::min<long long>((total_cells + threads - 1) / threads, 152LL * 16);
+      batched_combine0_kernel<T><<<blocks, threads, 0, st>>>(b, d_cum, ngrids, total_cells, nv, dim == 2, ns == 1);
+      CK(cudaGetLastError());
+    }
+    for (int s = 1; s < ns; ++s) {
+      BatchArgs<T> c = args(u);
+      c.stage = s;
+      c.last_stage = s == ns - 1;
+      c.want_emax = 0;
+      if (dim == 2) {
+        c.mode = 0;
+        c.dout_sel = 0;
+        int rc = launch_sweep(c, 0, slot++, st);
+        if (rc) return rc;
+        c.mode = 1;
+        rc = launch_sweep(c, 1, slot++, st);
+        if (rc) return rc;
+      } else {
+        c.mode = 2;
+        int rc = launch_sweep(c, 0, slot++, st);
+        if (rc) return rc;
+      }
+    }
+    end_step_kernel<<<(ngrids + 127) / 128, 128, 0, st>>>(clocks, ngrids);
+    CK(cudaGetLastError());
+    return ASTREA_OK;
+  }
+
+  int initialise(const void* prim, void* arena, cudaStream_t st) override {
+    const T* w = static_cast<const T*>(prim);
+    T* q = static_cast<T*>(arena);
+    for (int g = 0; g < ngrids; ++g) {
+      const astrea_grid& a = host_grids[g];
+      const long long base = (long long)nv * cum[g], cells = cum[g + 1] - cum[g];
+      const int n1 = dim == 1 ? 1 : a.n1;
+      const int ho = a.scheme >= PPM;
+      const int threads = 256;
+      const int blocks = (int)std::min<long long>((cells + threads - 1) / threads, 152LL * 8);
+      const T gm1 = T(a.gamma - 1.0);
+      if (model == 3) init_pass_a<T, 3><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
+      else if (model == 4) init_pass_a<T, 4><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
+      else init_pass_a<T, 8><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
+      CK(cudaGetLastError());
+      centre_to_avg_kernel<T><<<blocks, threads, 0, st>>>(tmp + base, q + base, a.n0, n1, cells, nv, dim, a.boundary);
+      CK(cudaGetLastError());
+    }
+    return ASTREA_OK;
+  }
+};
+
+extern "C" {
+
+int astrea_batch_create(int dim, int model, int precision, int integrator, const astrea_grid* grids, int ngrids,
+                        astrea_batch** out) {
+  if (!out || !grids || ngrids <= 0) return fail(ASTREA_ERR_ARG, "bad batch arguments");
+  *out = nullptr;
+  if (dim != 1 && dim != 2) return fail(ASTREA_ERR_CONFIG, "dim must be 1 or 2");
+  if (!((dim == 1 && (model == 3 || model == 8)) || (dim == 2 && (model == 4 || model == 8))))
+    return fail(ASTREA_ERR_CONFIG, "batch model must be 3|8 in 1D, 4|8 in 2D");
+  if (precision != 32 && precision != 64) return fail(ASTREA_ERR_CONFIG, "precision must be 32 or 64");
+  if (stages_count(integrator) < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported");
+  IBatch* b = precision == 64 ? static_cast<IBatch*>(new Batch<double>()) : static_cast<IBatch*>(new Batch<float>());
+  b->dim = dim;
+  b->model = model;
+  b->precision = precision;
+  b->integrator = integrator;
+  b->ngrids = ngrids;
+  b->nv = model;
+  b->host_grids.assign(grids, grids + ngrids);
+  b->cum.assign(ngrids + 1, 0);
+  for (int g = 0; g < ngrids; ++g) {
+    const astrea_grid& a = grids[g];
+    if (a.n0 < 4 || (dim == 2 && a.n1 < 4) || (dim == 1 && a.n1 != 1) || !(a.dx > 0) || !(a.cfl > 0) ||
+        !(a.gamma > 1) || a.checkpoints < 1 || (a.flags & ASTREA_FLAG_CT)) {
+      delete b;
+      return fail(ASTREA_ERR_CONFIG, "invalid grid in batch (sizes >= 4, dx, cfl > 0, gamma > 1; no constrained transport)");
+    }
+    b->cum[g + 1] = b->cum[g] + (long long)a.n0 * (dim == 2 ? a.n1 : 1);
+  }
+  b->total_cells = b->cum[ngrids];
+  std::vector<Clock> clk(ngrids);
+  for (int g = 0; g < ngrids; ++g) {
+    Clock& c = clk[g];
+    std::memset(&c, 0, sizeof(c));
+    c.t_end = grids[g].t_end;
+    c.chkpt = grids[g].t_end / grids[g].checkpoints;
+    c.cfl = grids[g].cfl;
+    c.dx = grids[g].dx;
+    c.idx = 1;
+    c.naxes = dim;
+  }
+  if (cudaMalloc(&b->clocks, sizeof(Clock) * ngrids) != cudaSuccess ||
+      cudaMalloc(&b->d_cum, sizeof(long long) * (ngrids + 1)) != cudaSuccess) {
+    delete b;
+    return fail(ASTREA_ERR_OOM, "batch clock allocation failed");
+  }
+  cudaMemcpy(b->clocks, clk.data(), sizeof(Clock) * ngrids, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_cum, b->cum.data(), sizeof(long long) * (ngrids + 1), cudaMemcpyHostToDevice);
+  int rc = b->alloc();
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  *out = new astrea_batch{b};
+  return ASTREA_OK;
+}
+
+void astrea_batch_destroy(astrea_batch* h) {
+  if (!h) return;
+  delete h->b;
+  delete h;
+}
+
+int astrea_batch_layout(const astrea_batch* h, long long* offsets, int* nv, long long* total_elems) {
+  if (!h) return fail(ASTREA_ERR_ARG, "batch is NULL");
+  IBatch* b = h->b;
+  if (offsets)
+    for (int g = 0; g <= b->ngrids; ++g) offsets[g] = (long long)b->nv * b->cum[g];
+  if (nv) *nv = b->nv;
+  if (total_elems) *total_elems = (long long)b->nv * b->total_cells;
+  return ASTREA_OK;
+}
+
+int astrea_batch_initialise(astrea_batch* h, const void* prim_arena, void* arena, void* stream) {
+  if (!h || !prim_arena || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
+  return h->b->initialise(prim_arena, arena, static_cast<cudaStream_t>(stream));
+}
+
+int astrea_batch_step(astrea_batch* h, void* arena, int nsteps, void* stream) {
+  if (!h || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
+  for (int i = 0; i < nsteps; ++i) {
+    int rc = h->b->enqueue_step(arena, static_cast<cudaStream_t>(stream));
+    if (rc) return rc;
+  }
+  return ASTREA_OK;
+}
+
+int astrea_batch_graph_step(astrea_batch* h, void* arena, int nsteps, void* stream) {
+  if (!h || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
+  IBatch* b = h->b;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!b->graph || b->graph_arena != arena) {
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+    cudaStream_t cap;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed));
+    int rc = b->enqueue_step(arena, cap);
+    cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+    b->graph_arena = arena;
+  }
+  for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(b->graph, st));
+  return ASTREA_OK;
+}
+
+int astrea_batch_clocks(astrea_batch* h, double* t, double* dt, int* steps, int* done, int* status, void* stream) {
+  if (!h) return fail(ASTREA_ERR_ARG, "batch is NULL");
+  IBatch* b = h->b;
+  std::vector<Clock> c(b->ngrids);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  CK(cudaMemcpyAsync(c.data(), b->clocks, sizeof(Clock) * b->ngrids, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int g = 0; g < b->ngrids; ++g) {
+    if (t) t[g] = c[g].t;
+    if (dt) dt[g] = c[g].dt;
+    if (steps) steps[g] = c[g].steps;
+    if (done) done[g] = c[g].done;
+    if (status) status[g] = c[g].status;
+  }
+  return ASTREA_OK;
+}
+
+}  // extern "C"

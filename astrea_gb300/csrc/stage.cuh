@@ -26,7 +26,7 @@ __global__ void combine0_kernel(const T* __restrict__ u, const T* __restrict__ d
 // dt = cfl * min over axes (in iteration order) of dx / eigmax, clipped to the
 // next checkpoint (astrea.py:70-78).  Python's min keeps the first of equal or
 // unordered values, which decides how a NaN speed propagates.
-__global__ void dt_kernel(Clock* clocks, int ngrids) {
+static __global__ void dt_kernel(Clock* clocks, int ngrids) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ngrids) return;
   Clock& c = clocks[g];
@@ -51,7 +51,7 @@ __global__ void dt_kernel(Clock* clocks, int ngrids) {
 // After the last stage: advance t, count the step, flip the axis order
 // (astrea.py:84-85), reset the speed maxima, and mark the run done once
 // t reaches t_end (astrea.py:45, 61-63).
-__global__ void end_step_kernel(Clock* clocks, int ngrids) {
+static __global__ void end_step_kernel(Clock* clocks, int ngrids) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ngrids) return;
   Clock& c = clocks[g];
@@ -220,7 +220,7 @@ __global__ void sums_pass1(const T* __restrict__ q, long long plane, long long n
   }
 }
 
-__global__ void sums_pass2(const double* __restrict__ part, int nblocks, int nv, double* __restrict__ out) {
+static __global__ void sums_pass2(const double* __restrict__ part, int nblocks, int nv, double* __restrict__ out) {
   const int s = threadIdx.x;
   if (s >= nv) return;
   double S = 0.0, Cc = 0.0;

@@ -128,15 +128,16 @@ template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, un
   }
 }
 
+// One tile: cells [s0, s0+TS) along the sweep and rows [t0, t0+TT) across it.
+// Called by the single-grid kernel (one tile per CTA) and by the batched
+// persistent kernel (a work list of tiles of many grids).
 template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT>
-__global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
+__device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, const int t0,
+                                           unsigned char* __restrict__ smem_raw) {
   using M = Model<MID>;
   using G = Geom<SCH, DIM, TS, TT>;
   using S = Smem<SCH, DIM, TS, TT, M::NV>;
   constexpr int NV = M::NV;
-  if (a.clock->done) return;
-
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   T* s_q = sm;                       // region 0 (a): q and its point primitives
   T* s_qw = s_q + S::n_q;
@@ -148,8 +149,6 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
 
   const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
   const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
-  const int s0 = blockIdx.x * TS;
-  const int t0 = blockIdx.y * TT;
   const Clamp rs_ = make_rho(a.bc, Ns);
   const Clamp rt_ = make_rho(a.bc, Nt);
   const T gamma = a.gamma, gm1 = a.gm1;
@@ -469,6 +468,13 @@ __global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
       }
     }
   }
+}
+
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT>
+__global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
+  if (a.clock->done) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT>(a, blockIdx.x * TS, blockIdx.y * TT, smem_raw);
 }
 
 }  // namespace astrea

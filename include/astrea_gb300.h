@@ -144,6 +144,37 @@ int astrea_to_primitive(astrea_handle* h, const void* state, void* prim_out, voi
  * the host).  sums_host receives nv doubles.  Synchronises ``stream``. */
 int astrea_reduce_conserved(astrea_handle* h, const void* state, double* sums_host, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Batched engine: many independent grids of uneven sizes in one state arena.
+ * The reference runs one grid per process (astrea.py:155-190 loops over
+ * resolutions sequentially); a batch advances every grid of the arena per
+ * call, each with its own dt/t/t_end, with one persistent kernel per sweep
+ * whose CTAs pull tiles of all grids from a work list.
+ * ------------------------------------------------------------------------ */
+typedef struct astrea_grid {
+  int n0, n1;          /* cells (n1 = 1 in 1D) */
+  int scheme;          /* ASTREA_PLM, ASTREA_PPM or ASTREA_WENO5 */
+  int solver;          /* ASTREA_LLF, or ASTREA_HLLC (Euler models) / ASTREA_HLLD (model 8) */
+  int boundary, limiter, flags;
+  double gamma, dx, cfl, t_end;
+  int checkpoints;
+} astrea_grid;
+
+typedef struct astrea_batch astrea_batch;
+
+/* All grids share dim, model (3|8 in 1D, 4|8 in 2D), precision and integrator. */
+int astrea_batch_create(int dim, int model, int precision, int integrator, const astrea_grid* grids, int ngrids,
+                        astrea_batch** out);
+void astrea_batch_destroy(astrea_batch* b);
+/* offsets (ngrids+1 elements): element offset of each grid's first plane in the
+ * arena; grid g holds nv planes of n0*n1 elements from offsets[g]. */
+int astrea_batch_layout(const astrea_batch* b, long long* offsets, int* nv, long long* total_elems);
+int astrea_batch_initialise(astrea_batch* b, const void* prim_arena, void* arena, void* stream);
+int astrea_batch_step(astrea_batch* b, void* arena, int nsteps, void* stream);
+int astrea_batch_graph_step(astrea_batch* b, void* arena, int nsteps, void* stream);
+/* per-grid clocks (arrays of ngrids; any may be NULL); synchronises ``stream`` */
+int astrea_batch_clocks(astrea_batch* b, double* t, double* dt, int* steps, int* done, int* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

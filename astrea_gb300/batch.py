@@ -26,11 +26,12 @@ class GridSpec(ctypes.Structure):
 
 
 _SIGS = {
-    "astrea_batch_create": ([ctypes.c_int] * 4 + [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "astrea_batch_create": ([ctypes.c_int] * 5 + [ctypes.c_longlong, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "astrea_batch_destroy": ([ctypes.c_void_p], None),
-    "astrea_batch_layout": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
-                             ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
-    "astrea_batch_initialise": ([ctypes.c_void_p] * 4, ctypes.c_int),
+    "astrea_batch_set": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong], ctypes.c_int),
+    "astrea_batch_clear": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "astrea_batch_initialise": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+                                ctypes.c_int),
     "astrea_batch_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "astrea_batch_graph_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "astrea_batch_clocks": ([ctypes.c_void_p] * 7, ctypes.c_int),
@@ -55,32 +56,26 @@ def spec_of(cfg: RunConfig):
                     checkpoints=cfg.checkpoints)
 
 
-class Batch:
-    def __init__(self, cfgs, device=None):
+class SlotBatch:
+    """A fixed-capacity batch whose slots are filled and released between steps."""
+
+    def __init__(self, dim, model, precision, integrator, max_slots, capacity_elems, device=None):
         if not torch.cuda.is_available():
             raise _lib.AstreaError(-2, "no CUDA device: the astrea_gb300 update runs only on the GPU")
-        c0 = cfgs[0]
-        for c in cfgs:
-            if (c.dim, c.model, c.precision, c.integrator) != (c0.dim, c0.model, c0.precision, c0.integrator):
-                raise C.ConfigError("a batch shares dim, model, precision and integrator")
-        self.cfgs = list(cfgs)
-        self.dim, self.model, self.precision = c0.dim, c0.model, c0.precision
+        self.dim, self.model, self.precision = dim, model, precision
+        self.max_slots = max_slots
         self.lib = _lib_batch()
         self.device = torch.device(device or "cuda")
-        specs = (GridSpec * len(cfgs))(*[spec_of(c) for c in cfgs])
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.astrea_batch_create(c0.dim, c0.model, c0.precision, C.INTEGRATOR[c0.integrator],
-                                                    ctypes.cast(specs, ctypes.c_void_p), len(cfgs), ctypes.byref(h)))
+            _lib.check(self.lib.astrea_batch_create(dim, model, precision, C.INTEGRATOR[integrator], max_slots,
+                                                    int(capacity_elems), ctypes.byref(h)))
         self.handle = h
-        offs = (ctypes.c_longlong * (len(cfgs) + 1))()
-        nv, total = ctypes.c_int(), ctypes.c_longlong()
-        _lib.check(self.lib.astrea_batch_layout(self.handle, ctypes.cast(offs, ctypes.c_void_p), ctypes.byref(nv),
-                                                ctypes.byref(total)))
-        self.offsets = list(offs)
-        self.nv = nv.value
-        dtype = torch.float64 if c0.precision == 64 else torch.float32
-        self.arena = torch.zeros(total.value, dtype=dtype, device=self.device)
+        self.nv = model
+        dtype = torch.float64 if precision == 64 else torch.float32
+        self.arena = torch.zeros(int(capacity_elems), dtype=dtype, device=self.device)
+        self.prim_arena = torch.zeros_like(self.arena)
+        self.slots = {}  # slot -> (cfg, offset)
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -92,41 +87,88 @@ class Batch:
             self.lib.astrea_batch_destroy(h)
             self.handle = None
 
-    def __len__(self):
-        return len(self.cfgs)
-
-    def planes(self, g):
-        """View (nv, n0, n1) of grid g's state in the arena."""
-        c = self.cfgs[g]
-        n1 = c.n1 if c.dim == 2 else 1
-        return self.arena[self.offsets[g]:self.offsets[g + 1]].view(self.nv, c.n0, n1)
-
-    def initialise(self, prims):
-        """Point primitives (one (n0[, n1], 8) array per grid) -> cell-averaged conservatives."""
-        prim_arena = torch.zeros_like(self.arena)
-        idx = MODEL_VARS[self.model]
-        for g, w in enumerate(prims):
-            t = torch.as_tensor(w)
-            if t.dim() == 2:
-                t = t[:, None, :]
-            prim_arena[self.offsets[g]:self.offsets[g + 1]].view(self.nv, *t.shape[:2]).copy_(
-                t[..., idx].permute(2, 0, 1).to(self.arena.dtype))
-        _lib.check(self.lib.astrea_batch_initialise(self.handle, ctypes.c_void_p(prim_arena.data_ptr()),
+    def occupy(self, slot, cfg, offset, w_point):
+        """Put grid ``cfg`` at element ``offset`` into ``slot`` and initialise it from point primitives."""
+        spec = spec_of(cfg)
+        _lib.check(self.lib.astrea_batch_set(self.handle, int(slot), ctypes.byref(spec), int(offset)))
+        self.slots[slot] = (cfg, int(offset))
+        t = torch.as_tensor(w_point)
+        if t.dim() == 2:
+            t = t[:, None, :]
+        n = self.nv * t.shape[0] * t.shape[1]
+        self.prim_arena[offset:offset + n].view(self.nv, t.shape[0], t.shape[1]).copy_(
+            t[..., MODEL_VARS[self.model]].permute(2, 0, 1).to(self.arena.dtype))
+        _lib.check(self.lib.astrea_batch_initialise(self.handle, int(slot), ctypes.c_void_p(self.prim_arena.data_ptr()),
                                                     ctypes.c_void_p(self.arena.data_ptr()), _stream()))
-        torch.cuda.current_stream().synchronize()
 
-    def step(self, n=1, graph=True):
+    def release(self, slot):
+        _lib.check(self.lib.astrea_batch_clear(self.handle, int(slot)))
+        self.slots.pop(slot, None)
+
+    def planes(self, slot):
+        cfg, off = self.slots[slot]
+        n1 = cfg.n1 if cfg.dim == 2 else 1
+        return self.arena[off:off + self.nv * cfg.n0 * n1].view(self.nv, cfg.n0, n1)
+
+    def step(self, n=1, graph=False):
         fn = self.lib.astrea_batch_graph_step if graph else self.lib.astrea_batch_step
         _lib.check(fn(self.handle, ctypes.c_void_p(self.arena.data_ptr()), int(n), _stream()))
 
     def clocks(self):
-        g = len(self.cfgs)
+        g = self.max_slots
         t, dt = (ctypes.c_double * g)(), (ctypes.c_double * g)()
         steps, done, status = (ctypes.c_int * g)(), (ctypes.c_int * g)(), (ctypes.c_int * g)()
         _lib.check(self.lib.astrea_batch_clocks(self.handle, *[ctypes.cast(x, ctypes.c_void_p) for x in
                                                                (t, dt, steps, done, status)], _stream()))
         return {"t": np.array(t[:]), "dt": np.array(dt[:]), "steps": np.array(steps[:]),
                 "done": np.array(done[:], dtype=bool), "status": np.array(status[:])}
+
+
+class Batch:
+    """A static batch: every grid occupies one slot of a packed arena."""
+
+    def __init__(self, cfgs, device=None):
+        c0 = cfgs[0]
+        for c in cfgs:
+            if (c.dim, c.model, c.precision, c.integrator) != (c0.dim, c0.model, c0.precision, c0.integrator):
+                raise C.ConfigError("a batch shares dim, model, precision and integrator")
+        self.cfgs = list(cfgs)
+        self.dim, self.model, self.precision = c0.dim, c0.model, c0.precision
+        self.nv = c0.model
+        sizes = [self.nv * c.n0 * (c.n1 if c.dim == 2 else 1) for c in cfgs]
+        self.offsets = [0] + list(np.cumsum(sizes))
+        self.sb = SlotBatch(c0.dim, c0.model, c0.precision, c0.integrator, len(cfgs), self.offsets[-1], device)
+        self.arena = self.sb.arena
+        for g, c in enumerate(cfgs):
+            _lib.check(self.sb.lib.astrea_batch_set(self.sb.handle, g, ctypes.byref(spec_of(c)),
+                                                    int(self.offsets[g])))
+            self.sb.slots[g] = (c, int(self.offsets[g]))
+
+    def __len__(self):
+        return len(self.cfgs)
+
+    def planes(self, g):
+        return self.sb.planes(g)
+
+    def initialise(self, prims):
+        for g, w in enumerate(prims):
+            cfg, off = self.sb.slots[g]
+            t = torch.as_tensor(w)
+            if t.dim() == 2:
+                t = t[:, None, :]
+            n = self.nv * t.shape[0] * t.shape[1]
+            self.sb.prim_arena[off:off + n].view(self.nv, t.shape[0], t.shape[1]).copy_(
+                t[..., MODEL_VARS[self.model]].permute(2, 0, 1).to(self.arena.dtype))
+            _lib.check(self.sb.lib.astrea_batch_initialise(self.sb.handle, g,
+                                                           ctypes.c_void_p(self.sb.prim_arena.data_ptr()),
+                                                           ctypes.c_void_p(self.arena.data_ptr()), _stream()))
+        torch.cuda.current_stream().synchronize()
+
+    def step(self, n=1, graph=True):
+        self.sb.step(n, graph=graph)
+
+    def clocks(self):
+        return self.sb.clocks()
 
     def run(self, max_steps=None, check_every=16, graph=True):
         n = 0

@@ -98,28 +98,25 @@ __global__ void __launch_bounds__(256) batched_sweep_kernel(const BatchArgs<T> b
   }
 }
 
-// stage-0 combine over all grids: thread -> (grid, cell) by binary search of the cell offsets
+// stage-0 combine over all grids: one CTA per tile of the axis-0 work list
 template <typename T>
-__global__ void batched_combine0_kernel(const BatchArgs<T> b, const long long* __restrict__ cum, int ngrids,
-                                        long long total, int nv, int dim2, int single_stage) {
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < total; c += (long long)gridDim.x * blockDim.x) {
-    int lo = 0, hi = ngrids - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (cum[mid] <= c) lo = mid; else hi = mid - 1;
-    }
-    const int g = lo;
-    const Clock& clk = b.clocks[g];
-    if (clk.done) continue;
-    const BGrid<T>& gd = b.grids[g];
-    const long long cell = c - cum[g];
-    const T dt = T(clk.dt);
-    T* out = single_stage ? b.u : b.k0;
+__global__ void batched_combine0_kernel(const BatchArgs<T> b, const BItem* __restrict__ items, int nv, int dim2,
+                                        int single_stage, int TS, int TT) {
+  const BItem w = items[blockIdx.x];
+  const Clock& clk = b.clocks[w.g];
+  if (clk.done) return;
+  const BGrid<T>& gd = b.grids[w.g];
+  const T dt = T(clk.dt);
+  T* out = single_stage ? b.u : b.k0;
+  for (int e = threadIdx.x; e < TS * TT; e += blockDim.x) {
+    const int i = w.s0 + e / TT, j = w.t0 + e % TT;  // axis-0 frame: i along n0, j along n1 (contiguous)
+    if (i >= gd.n0 || j >= gd.n1) continue;
+    const long long cell = (long long)i * gd.n1 + j;
     for (int s = 0; s < nv; ++s) {
-      const long long e = gd.base + s * gd.cells + cell;
-      const T total_ = dim2 ? b.d0[e] + b.d1[e] : b.d0[e];
+      const long long e2 = gd.base + s * gd.cells + cell;
+      const T total_ = dim2 ? b.d0[e2] + b.d1[e2] : b.d0[e2];
       const T L = -total_;
-      out[e] = combine<T>(b.integ, 0, b.u[e], b.u[e], L, dt);
+      out[e2] = combine<T>(b.integ, 0, b.u[e2], b.u[e2], L, dt);
     }
   }
 }

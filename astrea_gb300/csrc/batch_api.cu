@@ -1,5 +1,11 @@
-// C ABI of the batched engine (astrea_batch_*): many independent grids in
-// one state arena, advanced together with persistent sweep kernels.
+// C ABI of the batched engine (astrea_batch_*).
+//
+// A batch owns a fixed number of *slots* and stage buffers for a fixed arena
+// capacity.  A slot holds one grid at a caller-chosen element offset of the
+// caller's state arena; slots are occupied and released at any time between
+// steps (continuous batching).  Each step advances every occupied, unfinished
+// slot by one of its own time steps: one persistent kernel per sweep walks a
+// work list of tiles of all occupied slots (largest grids first).
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -37,38 +43,7 @@ int combo_of(int scheme, int solver, int model, int* out) {
   }
 }
 
-}  // namespace
-
-struct IBatch {
-  int dim = 2, model = 4, precision = 32, integrator = SSPRK33, ngrids = 0, nv = 0;
-  std::vector<astrea_grid> host_grids;
-  std::vector<long long> cum;  // cell offsets, ngrids + 1
-  long long total_cells = 0;
-  Clock* clocks = nullptr;
-  long long* d_cum = nullptr;
-  int* counters = nullptr;  // one work counter per sweep launch of a step
-  BItem* items[2] = {nullptr, nullptr};
-  int nitems[2] = {0, 0};
-  cudaGraphExec_t graph = nullptr;
-  void* graph_arena = nullptr;
-  virtual ~IBatch() {
-    if (graph) cudaGraphExecDestroy(graph);
-    cudaFree(clocks);
-    cudaFree(d_cum);
-    cudaFree(counters);
-    cudaFree(items[0]);
-    cudaFree(items[1]);
-  }
-  virtual int alloc() = 0;
-  virtual int enqueue_step(void* arena, cudaStream_t st) = 0;
-  virtual int initialise(const void* prim, void* arena, cudaStream_t st) = 0;
-};
-
-struct astrea_batch {
-  IBatch* b;
-};
-
-static int stages_count(int integ) {
+int stages_count(int integ) {
   switch (integ) {
     case EULER: return 1;
     case SSPRK22: return 2;
@@ -78,51 +53,96 @@ static int stages_count(int integ) {
   }
 }
 
+}  // namespace
+
+struct IBatch {
+  int dim = 2, model = 4, precision = 32, integrator = SSPRK33, max_slots = 0, nv = 0;
+  long long capacity = 0;  // elements per arena
+  std::vector<astrea_grid> host_grids;
+  std::vector<long long> offsets;
+  std::vector<char> active;
+  bool dirty = true;
+  Clock* clocks = nullptr;
+  int* counters = nullptr;
+  BItem* items[2] = {nullptr, nullptr};
+  size_t items_cap[2] = {0, 0};
+  int nitems[2] = {0, 0};
+  cudaGraphExec_t graph = nullptr;
+  void* graph_arena = nullptr;
+  virtual ~IBatch() {
+    if (graph) cudaGraphExecDestroy(graph);
+    cudaFree(clocks);
+    cudaFree(counters);
+    cudaFree(items[0]);
+    cudaFree(items[1]);
+  }
+  virtual int alloc() = 0;
+  virtual int set_slot(int slot, const astrea_grid& g, long long offset) = 0;
+  virtual int rebuild() = 0;
+  virtual int enqueue_step(void* arena, cudaStream_t st) = 0;
+  virtual int initialise(int slot, const void* prim, void* arena, cudaStream_t st) = 0;
+};
+
+struct astrea_batch {
+  IBatch* b;
+};
+
 template <typename T> struct Batch final : IBatch {
-  T* k0 = nullptr;
-  T* k1 = nullptr;
-  T* d0 = nullptr;
-  T* d1 = nullptr;
-  T* tmp = nullptr;
+  T *k0 = nullptr, *k1 = nullptr, *d0 = nullptr, *d1 = nullptr, *tmp = nullptr;
   BGrid<T>* d_grids = nullptr;
   BatchFn<T> sweep[2] = {nullptr, nullptr};
   int nctas[2] = {0, 0};
+  int occ[2] = {1, 1};
+  int sms = 152;
 
   ~Batch() override {
     cudaFree(k0); cudaFree(k1); cudaFree(d0); cudaFree(d1); cudaFree(tmp); cudaFree(d_grids);
   }
 
   int alloc() override {
-    const size_t bytes = sizeof(T) * (size_t)nv * (size_t)total_cells;
+    const size_t bytes = sizeof(T) * (size_t)capacity;
     if (cudaMalloc(&k0, bytes) != cudaSuccess || cudaMalloc(&k1, bytes) != cudaSuccess ||
         cudaMalloc(&d0, bytes) != cudaSuccess || cudaMalloc(&d1, bytes) != cudaSuccess ||
         cudaMalloc(&tmp, bytes) != cudaSuccess)
       return fail(ASTREA_ERR_OOM, "batch stage buffers allocation failed");
-    std::vector<BGrid<T>> hg(ngrids);
-    for (int g = 0; g < ngrids; ++g) {
-      const astrea_grid& a = host_grids[g];
-      BGrid<T>& d = hg[g];
-      d.base = (long long)nv * cum[g];
-      d.cells = cum[g + 1] - cum[g];
-      d.n0 = a.n0;
-      d.n1 = dim == 1 ? 1 : a.n1;
-      d.bc = a.boundary;
-      d.limiter = a.limiter;
-      d.physical = (a.flags & ASTREA_FLAG_PHYSICAL) ? 1 : 0;
-      if (combo_of(a.scheme, a.solver, model, &d.combo)) return fail(ASTREA_ERR_CONFIG, "batch grid has an unsupported scheme/solver");
-      d.gamma = T(a.gamma);
-      d.gm1 = T(a.gamma - 1.0);
-      d.dx = a.dx;
-    }
-    CK(cudaMalloc(&d_grids, sizeof(BGrid<T>) * ngrids));
-    CK(cudaMemcpy(d_grids, hg.data(), sizeof(BGrid<T>) * ngrids, cudaMemcpyHostToDevice));
-    // work lists, largest grids first
-    std::vector<int> order(ngrids);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cum[x + 1] - cum[x] > cum[y + 1] - cum[y]; });
-    int dev_sms = 0, dev = 0;
+    CK(cudaMalloc(&d_grids, sizeof(BGrid<T>) * max_slots));
+    CK(cudaMalloc(&counters, sizeof(int) * 16));
+    int dev = 0;
     CK(cudaGetDevice(&dev));
-    CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    for (int ax = 0; ax < dim; ++ax) {
+      sweep[ax] = batched_for<T>(model, dim, ax);
+      if (!sweep[ax]) return fail(ASTREA_ERR_CONFIG, "no batched kernel for this model/dimension");
+      BatchArgs<T> probe{};
+      CK(sweep[ax](probe, 0, nullptr));
+      occ[ax] = std::max(1, occupancy_for<T>(model, dim, ax));
+    }
+    return ASTREA_OK;
+  }
+
+  int set_slot(int slot, const astrea_grid& a, long long offset) override {
+    BGrid<T> d{};
+    d.base = offset;
+    d.cells = (long long)a.n0 * (dim == 2 ? a.n1 : 1);
+    d.n0 = a.n0;
+    d.n1 = dim == 1 ? 1 : a.n1;
+    d.bc = a.boundary;
+    d.limiter = a.limiter;
+    d.physical = (a.flags & ASTREA_FLAG_PHYSICAL) ? 1 : 0;
+    if (combo_of(a.scheme, a.solver, model, &d.combo)) return fail(ASTREA_ERR_CONFIG, "unsupported scheme/solver for a batch");
+    d.gamma = T(a.gamma);
+    d.gm1 = T(a.gamma - 1.0);
+    d.dx = a.dx;
+    CK(cudaMemcpy(d_grids + slot, &d, sizeof(d), cudaMemcpyHostToDevice));
+    return ASTREA_OK;
+  }
+
+  int rebuild() override {
+    std::vector<int> order;
+    for (int s = 0; s < max_slots; ++s)
+      if (active[s]) order.push_back(s);
+    auto cells = [&](int s) { return (long long)host_grids[s].n0 * (dim == 2 ? host_grids[s].n1 : 1); };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells(x) > cells(y); });
     for (int ax = 0; ax < dim; ++ax) {
       const int TS = dim == 1 ? BTS1 : BTS2, TT = dim == 1 ? 1 : BTT2;
       std::vector<BItem> it;
@@ -134,16 +154,16 @@ template <typename T> struct Batch final : IBatch {
           for (int t0 = 0; t0 < Nt; t0 += TT) it.push_back(BItem{g, s0, t0});
       }
       nitems[ax] = (int)it.size();
-      CK(cudaMalloc(&items[ax], sizeof(BItem) * it.size()));
-      CK(cudaMemcpy(items[ax], it.data(), sizeof(BItem) * it.size(), cudaMemcpyHostToDevice));
-      sweep[ax] = batched_for<T>(model, dim, ax);
-      if (!sweep[ax]) return fail(ASTREA_ERR_CONFIG, "no batched kernel for this model/dimension");
-      BatchArgs<T> probe{};
-      CK(sweep[ax](probe, 0, nullptr));
-      const int occ = std::max(1, occupancy_for<T>(model, dim, ax));
-      nctas[ax] = std::max(1, std::min(nitems[ax], occ * dev_sms));
+      if (it.size() > items_cap[ax]) {
+        cudaFree(items[ax]);
+        items[ax] = nullptr;
+        items_cap[ax] = std::max<size_t>(it.size(), 2 * items_cap[ax]);
+        CK(cudaMalloc(&items[ax], sizeof(BItem) * items_cap[ax]));
+      }
+      if (!it.empty()) CK(cudaMemcpy(items[ax], it.data(), sizeof(BItem) * it.size(), cudaMemcpyHostToDevice));
+      nctas[ax] = std::max(1, std::min(nitems[ax], occ[ax] * sms));
     }
-    CK(cudaMalloc(&counters, sizeof(int) * 16));
+    dirty = false;
     return ASTREA_OK;
   }
 
@@ -161,6 +181,7 @@ template <typename T> struct Batch final : IBatch {
   }
 
   int launch_sweep(BatchArgs<T> b, int ax, int slot, cudaStream_t st) {
+    if (nitems[ax] == 0) return ASTREA_OK;
     b.items = items[ax];
     b.nitems = nitems[ax];
     b.counter = counters + slot;
@@ -170,11 +191,14 @@ template <typename T> struct Batch final : IBatch {
   }
 
   int enqueue_step(void* arena, cudaStream_t st) override {
+    if (dirty) {
+      int rc = rebuild();
+      if (rc) return rc;
+    }
     T* u = static_cast<T*>(arena);
     const int ns = stages_count(integrator);
     int slot = 0;
     BatchArgs<T> b = args(u);
-    // stage 0
     b.stage = 0;
     b.mode = 0;
     b.want_emax = 1;
@@ -183,19 +207,17 @@ template <typename T> struct Batch final : IBatch {
       int rc = launch_sweep(b, ax, slot++, st);
       if (rc) return rc;
     }
-    dt_kernel<<<(ngrids + 127) / 128, 128, 0, st>>>(clocks, ngrids);
+    dt_kernel<<<(max_slots + 127) / 128, 128, 0, st>>>(clocks, max_slots);
     CK(cudaGetLastError());
-    {
-      const int threads = 256;
-      const int blocks = (int)std::min<long long>((total_cells + threads - 1) / threads, 152LL * 16);
-      batched_combine0_kernel<T><<<blocks, threads, 0, st>>>(b, d_cum, ngrids, total_cells, nv, dim == 2, ns == 1);
+    if (nitems[0] > 0) {
+      const int TS = dim == 1 ? BTS1 : BTS2, TT = dim == 1 ? 1 : BTT2;
+      batched_combine0_kernel<T><<<nitems[0], 256, 0, st>>>(b, items[0], nv, dim == 2, ns == 1, TS, TT);
       CK(cudaGetLastError());
     }
     for (int s = 1; s < ns; ++s) {
       BatchArgs<T> c = args(u);
       c.stage = s;
       c.last_stage = s == ns - 1;
-      c.want_emax = 0;
       if (dim == 2) {
         c.mode = 0;
         c.dout_sel = 0;
@@ -210,38 +232,43 @@ template <typename T> struct Batch final : IBatch {
         if (rc) return rc;
       }
     }
-    end_step_kernel<<<(ngrids + 127) / 128, 128, 0, st>>>(clocks, ngrids);
+    end_step_kernel<<<(max_slots + 127) / 128, 128, 0, st>>>(clocks, max_slots);
     CK(cudaGetLastError());
     return ASTREA_OK;
   }
 
-  int initialise(const void* prim, void* arena, cudaStream_t st) override {
+  int initialise(int slot, const void* prim, void* arena, cudaStream_t st) override {
     const T* w = static_cast<const T*>(prim);
     T* q = static_cast<T*>(arena);
-    for (int g = 0; g < ngrids; ++g) {
-      const astrea_grid& a = host_grids[g];
-      const long long base = (long long)nv * cum[g], cells = cum[g + 1] - cum[g];
-      const int n1 = dim == 1 ? 1 : a.n1;
-      const int ho = a.scheme >= PPM;
-      const int threads = 256;
-      const int blocks = (int)std::min<long long>((cells + threads - 1) / threads, 152LL * 8);
-      const T gm1 = T(a.gamma - 1.0);
-      if (model == 3) init_pass_a<T, 3><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
-      else if (model == 4) init_pass_a<T, 4><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
-      else init_pass_a<T, 8><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
-      CK(cudaGetLastError());
-      centre_to_avg_kernel<T><<<blocks, threads, 0, st>>>(tmp + base, q + base, a.n0, n1, cells, nv, dim, a.boundary);
-      CK(cudaGetLastError());
-    }
+    const astrea_grid& a = host_grids[slot];
+    const long long base = offsets[slot], cells = (long long)a.n0 * (dim == 2 ? a.n1 : 1);
+    const int n1 = dim == 1 ? 1 : a.n1;
+    const int ho = a.scheme >= PPM;
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>((cells + threads - 1) / threads, 152LL * 8);
+    const T gm1 = T(a.gamma - 1.0);
+    if (model == 3) init_pass_a<T, 3><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
+    else if (model == 4) init_pass_a<T, 4><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
+    else init_pass_a<T, 8><<<blocks, threads, 0, st>>>(w + base, tmp + base, a.n0, n1, cells, dim, a.boundary, ho, gm1);
+    CK(cudaGetLastError());
+    centre_to_avg_kernel<T><<<blocks, threads, 0, st>>>(tmp + base, q + base, a.n0, n1, cells, nv, dim, a.boundary);
+    CK(cudaGetLastError());
     return ASTREA_OK;
   }
 };
 
+static int check_grid(int dim, const astrea_grid& a) {
+  if (a.n0 < 4 || (dim == 2 && a.n1 < 4) || (dim == 1 && a.n1 != 1) || !(a.dx > 0) || !(a.cfl > 0) || !(a.gamma > 1) ||
+      a.checkpoints < 1 || (a.flags & ASTREA_FLAG_CT))
+    return fail(ASTREA_ERR_CONFIG, "invalid grid (sizes >= 4, n1 == 1 in 1D, dx, cfl > 0, gamma > 1; no constrained transport)");
+  return ASTREA_OK;
+}
+
 extern "C" {
 
-int astrea_batch_create(int dim, int model, int precision, int integrator, const astrea_grid* grids, int ngrids,
+int astrea_batch_create(int dim, int model, int precision, int integrator, int max_slots, long long capacity_elems,
                         astrea_batch** out) {
-  if (!out || !grids || ngrids <= 0) return fail(ASTREA_ERR_ARG, "bad batch arguments");
+  if (!out || max_slots <= 0 || capacity_elems <= 0) return fail(ASTREA_ERR_ARG, "bad batch arguments");
   *out = nullptr;
   if (dim != 1 && dim != 2) return fail(ASTREA_ERR_CONFIG, "dim must be 1 or 2");
   if (!((dim == 1 && (model == 3 || model == 8)) || (dim == 2 && (model == 4 || model == 8))))
@@ -253,38 +280,20 @@ int astrea_batch_create(int dim, int model, int precision, int integrator, const
   b->model = model;
   b->precision = precision;
   b->integrator = integrator;
-  b->ngrids = ngrids;
+  b->max_slots = max_slots;
   b->nv = model;
-  b->host_grids.assign(grids, grids + ngrids);
-  b->cum.assign(ngrids + 1, 0);
-  for (int g = 0; g < ngrids; ++g) {
-    const astrea_grid& a = grids[g];
-    if (a.n0 < 4 || (dim == 2 && a.n1 < 4) || (dim == 1 && a.n1 != 1) || !(a.dx > 0) || !(a.cfl > 0) ||
-        !(a.gamma > 1) || a.checkpoints < 1 || (a.flags & ASTREA_FLAG_CT)) {
-      delete b;
-      return fail(ASTREA_ERR_CONFIG, "invalid grid in batch (sizes >= 4, dx, cfl > 0, gamma > 1; no constrained transport)");
-    }
-    b->cum[g + 1] = b->cum[g] + (long long)a.n0 * (dim == 2 ? a.n1 : 1);
-  }
-  b->total_cells = b->cum[ngrids];
-  std::vector<Clock> clk(ngrids);
-  for (int g = 0; g < ngrids; ++g) {
-    Clock& c = clk[g];
-    std::memset(&c, 0, sizeof(c));
-    c.t_end = grids[g].t_end;
-    c.chkpt = grids[g].t_end / grids[g].checkpoints;
-    c.cfl = grids[g].cfl;
-    c.dx = grids[g].dx;
-    c.idx = 1;
-    c.naxes = dim;
-  }
-  if (cudaMalloc(&b->clocks, sizeof(Clock) * ngrids) != cudaSuccess ||
-      cudaMalloc(&b->d_cum, sizeof(long long) * (ngrids + 1)) != cudaSuccess) {
+  b->capacity = capacity_elems;
+  b->host_grids.assign(max_slots, astrea_grid{});
+  b->offsets.assign(max_slots, 0);
+  b->active.assign(max_slots, 0);
+  std::vector<Clock> clk(max_slots);
+  std::memset(clk.data(), 0, sizeof(Clock) * max_slots);
+  for (auto& c : clk) c.done = 1;  // empty slots are skipped by every kernel
+  if (cudaMalloc(&b->clocks, sizeof(Clock) * max_slots) != cudaSuccess) {
     delete b;
     return fail(ASTREA_ERR_OOM, "batch clock allocation failed");
   }
-  cudaMemcpy(b->clocks, clk.data(), sizeof(Clock) * ngrids, cudaMemcpyHostToDevice);
-  cudaMemcpy(b->d_cum, b->cum.data(), sizeof(long long) * (ngrids + 1), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->clocks, clk.data(), sizeof(Clock) * max_slots, cudaMemcpyHostToDevice);
   int rc = b->alloc();
   if (rc) {
     delete b;
@@ -300,19 +309,48 @@ void astrea_batch_destroy(astrea_batch* h) {
   delete h;
 }
 
-int astrea_batch_layout(const astrea_batch* h, long long* offsets, int* nv, long long* total_elems) {
-  if (!h) return fail(ASTREA_ERR_ARG, "batch is NULL");
+int astrea_batch_set(astrea_batch* h, int slot, const astrea_grid* grid, long long offset) {
+  if (!h || !grid) return fail(ASTREA_ERR_ARG, "NULL argument");
   IBatch* b = h->b;
-  if (offsets)
-    for (int g = 0; g <= b->ngrids; ++g) offsets[g] = (long long)b->nv * b->cum[g];
-  if (nv) *nv = b->nv;
-  if (total_elems) *total_elems = (long long)b->nv * b->total_cells;
+  if (slot < 0 || slot >= b->max_slots) return fail(ASTREA_ERR_ARG, "slot out of range");
+  int rc = check_grid(b->dim, *grid);
+  if (rc) return rc;
+  const long long need = (long long)b->nv * grid->n0 * (b->dim == 2 ? grid->n1 : 1);
+  if (offset < 0 || offset + need > b->capacity) return fail(ASTREA_ERR_OOM, "grid does not fit in the batch arena");
+  b->host_grids[slot] = *grid;
+  b->offsets[slot] = offset;
+  rc = b->set_slot(slot, *grid, offset);
+  if (rc) return rc;
+  Clock c;
+  std::memset(&c, 0, sizeof(c));
+  c.t_end = grid->t_end;
+  c.chkpt = grid->t_end / grid->checkpoints;
+  c.cfl = grid->cfl;
+  c.dx = grid->dx;
+  c.idx = 1;
+  c.naxes = b->dim;
+  c.done = !(0.0 < grid->t_end);
+  CK(cudaMemcpy(b->clocks + slot, &c, sizeof(c), cudaMemcpyHostToDevice));
+  b->active[slot] = 1;
+  b->dirty = true;
   return ASTREA_OK;
 }
 
-int astrea_batch_initialise(astrea_batch* h, const void* prim_arena, void* arena, void* stream) {
+int astrea_batch_clear(astrea_batch* h, int slot) {
+  if (!h) return fail(ASTREA_ERR_ARG, "NULL argument");
+  IBatch* b = h->b;
+  if (slot < 0 || slot >= b->max_slots) return fail(ASTREA_ERR_ARG, "slot out of range");
+  int one = 1;
+  CK(cudaMemcpy(&b->clocks[slot].done, &one, sizeof(int), cudaMemcpyHostToDevice));
+  b->active[slot] = 0;
+  b->dirty = true;
+  return ASTREA_OK;
+}
+
+int astrea_batch_initialise(astrea_batch* h, int slot, const void* prim_arena, void* arena, void* stream) {
   if (!h || !prim_arena || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
-  return h->b->initialise(prim_arena, arena, static_cast<cudaStream_t>(stream));
+  if (slot < 0 || slot >= h->b->max_slots || !h->b->active[slot]) return fail(ASTREA_ERR_ARG, "slot not occupied");
+  return h->b->initialise(slot, prim_arena, arena, static_cast<cudaStream_t>(stream));
 }
 
 int astrea_batch_step(astrea_batch* h, void* arena, int nsteps, void* stream) {
@@ -328,10 +366,14 @@ int astrea_batch_graph_step(astrea_batch* h, void* arena, int nsteps, void* stre
   if (!h || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
   IBatch* b = h->b;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (!b->graph || b->graph_arena != arena) {
+  if (b->dirty || !b->graph || b->graph_arena != arena) {
     if (b->graph) {
       cudaGraphExecDestroy(b->graph);
       b->graph = nullptr;
+    }
+    if (b->dirty) {
+      int rc = b->rebuild();
+      if (rc) return rc;
     }
     cudaStream_t cap;
     CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -354,11 +396,11 @@ int astrea_batch_graph_step(astrea_batch* h, void* arena, int nsteps, void* stre
 int astrea_batch_clocks(astrea_batch* h, double* t, double* dt, int* steps, int* done, int* status, void* stream) {
   if (!h) return fail(ASTREA_ERR_ARG, "batch is NULL");
   IBatch* b = h->b;
-  std::vector<Clock> c(b->ngrids);
+  std::vector<Clock> c(b->max_slots);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  CK(cudaMemcpyAsync(c.data(), b->clocks, sizeof(Clock) * b->ngrids, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(c.data(), b->clocks, sizeof(Clock) * b->max_slots, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  for (int g = 0; g < b->ngrids; ++g) {
+  for (int g = 0; g < b->max_slots; ++g) {
     if (t) t[g] = c[g].t;
     if (dt) dt[g] = c[g].dt;
     if (steps) steps[g] = c[g].steps;

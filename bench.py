@@ -217,6 +217,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--cpu-n", type=int, default=192)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only-fp32", action="store_true",
+                    help="time the FP32 path only (no FP64, e2e or CPU legs); used for profiler captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -265,6 +267,16 @@ def main():
     achieved = alg_per_launch / (sweep_ms / max(sweep_launches, 1) / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     step_alg = cells * 8 * C * sz  # 8 state passes per SSPRK3 step (minimum traffic)
+
+    if args.only_fp32:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                              "config": {"workload": WORKLOAD, "cells": cells}, "only_fp32": True,
+                              "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1],
+                                            "bookkeeping": kernel_ms[2]}, "roofline_achieved_gbs": achieved}),
+                  flush=True)
+        return 0
 
     # ---- FP64 plain, same workload, and L1(rho) of FP32 against it after the same steps
     s64 = Solver(run_config(n, 64))

@@ -147,9 +147,11 @@ int astrea_reduce_conserved(astrea_handle* h, const void* state, double* sums_ho
 /* ------------------------------------------------------------------------
  * Batched engine: many independent grids of uneven sizes in one state arena.
  * The reference runs one grid per process (astrea.py:155-190 loops over
- * resolutions sequentially); a batch advances every grid of the arena per
- * call, each with its own dt/t/t_end, with one persistent kernel per sweep
- * whose CTAs pull tiles of all grids from a work list.
+ * resolutions one after another); a batch advances every occupied slot per
+ * call, each grid with its own dt/t/t_end, with one persistent kernel per
+ * sweep whose CTAs pull tiles of all grids from a work list.  Slots can be
+ * occupied and released between steps (continuous batching).  No
+ * counterpart in the reference.
  * ------------------------------------------------------------------------ */
 typedef struct astrea_grid {
   int n0, n1;          /* cells (n1 = 1 in 1D) */
@@ -162,17 +164,24 @@ typedef struct astrea_grid {
 
 typedef struct astrea_batch astrea_batch;
 
-/* All grids share dim, model (3|8 in 1D, 4|8 in 2D), precision and integrator. */
-int astrea_batch_create(int dim, int model, int precision, int integrator, const astrea_grid* grids, int ngrids,
+/* A batch of up to max_slots grids sharing dim, model (3|8 in 1D, 4|8 in 2D),
+ * precision and integrator, with stage buffers for capacity_elems elements
+ * of state (the caller's arena has the same size). */
+int astrea_batch_create(int dim, int model, int precision, int integrator, int max_slots, long long capacity_elems,
                         astrea_batch** out);
 void astrea_batch_destroy(astrea_batch* b);
-/* offsets (ngrids+1 elements): element offset of each grid's first plane in the
- * arena; grid g holds nv planes of n0*n1 elements from offsets[g]. */
-int astrea_batch_layout(const astrea_batch* b, long long* offsets, int* nv, long long* total_elems);
-int astrea_batch_initialise(astrea_batch* b, const void* prim_arena, void* arena, void* stream);
+/* Occupy ``slot`` with a grid whose nv planes start at element ``offset`` of
+ * the arena; resets the slot's clock to t = 0.  ASTREA_ERR_OOM if it does not fit. */
+int astrea_batch_set(astrea_batch* b, int slot, const astrea_grid* grid, long long offset);
+/* Release ``slot`` (its grid is no longer advanced). */
+int astrea_batch_clear(astrea_batch* b, int slot);
+/* Point primitives -> cell-averaged conservatives for one slot; ``prim_arena``
+ * holds the primitives at the slot's offset. */
+int astrea_batch_initialise(astrea_batch* b, int slot, const void* prim_arena, void* arena, void* stream);
 int astrea_batch_step(astrea_batch* b, void* arena, int nsteps, void* stream);
+/* As astrea_batch_step with one CUDA graph per step (recaptured after set/clear). */
 int astrea_batch_graph_step(astrea_batch* b, void* arena, int nsteps, void* stream);
-/* per-grid clocks (arrays of ngrids; any may be NULL); synchronises ``stream`` */
+/* Per-slot clocks (arrays of max_slots; any may be NULL); synchronises ``stream``. */
 int astrea_batch_clocks(astrea_batch* b, double* t, double* dt, int* steps, int* done, int* status, void* stream);
 
 #ifdef __cplusplus

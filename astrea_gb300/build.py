@@ -40,7 +40,8 @@ def sources():
 
 def flags_for(name):
     if name.startswith(("sweep_f32", "batch_k_f32")):
-        return ["--fmad=true"]
+        # FP32 path: fused multiply-add, approximate division and square root, flush-to-zero
+        return ["--fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
     return ["--fmad=false"]
 
 

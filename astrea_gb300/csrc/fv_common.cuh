@@ -26,6 +26,10 @@ template <typename T> __device__ __forceinline__ bool isnan_(T a) { return a != 
 // np.maximum / np.minimum: NaN in either operand gives NaN
 template <typename T> __device__ __forceinline__ T npmax(T a, T b) { return (a > b || isnan_(a)) ? a : b; }
 template <typename T> __device__ __forceinline__ T npmin(T a, T b) { return (a < b || isnan_(a)) ? a : b; }
+// FP32 path: one min/max instruction; a NaN operand is dropped instead of propagated
+// (the FP32 path is checked against FP64 by error norms, not bit for bit)
+template <> __device__ __forceinline__ float npmax<float>(float a, float b) { return fmaxf(a, b); }
+template <> __device__ __forceinline__ float npmin<float>(float a, float b) { return fminf(a, b); }
 // np.sign: -1, 0 (keeps the zero's sign), +1, NaN
 template <typename T> __device__ __forceinline__ T npsign(T a) { return a > T(0) ? T(1) : (a < T(0) ? T(-1) : a); }
 // fv.divide: a/b where b != 0 else 0
@@ -45,6 +49,10 @@ template <> __device__ __forceinline__ float abs_<float>(float a) { return fabsf
 struct Clamp {
   int lo, hi;
   __device__ __forceinline__ int operator()(int v) const { return v < lo ? lo : (v > hi ? hi : v); }
+};
+// tiles whose every level stays inside the grid (or periodic grids) need no clamping
+struct NoClamp {
+  __device__ __forceinline__ int operator()(int v) const { return v; }
 };
 __device__ __forceinline__ Clamp make_rho(int bc, int n) {
   Clamp c;

@@ -21,8 +21,8 @@ template <> struct Reach<WENO5> { static constexpr int L = 2, R = 2; };
 template <> struct Reach<WENO7> { static constexpr int L = 3, R = 3; };
 
 // PLM with minmod (limiters.py:10-19) or superbee (limiters.py:47-49) slopes; plm.py:26-36
-template <typename T, class A>
-__device__ __forceinline__ void recon_plm(const A& at, const Clamp& rho, int r, int limiter, T& wL, T& wR) {
+template <typename T, class A, class RH>
+__device__ __forceinline__ void recon_plm(const A& at, const RH& rho, int r, int limiter, T& wL, T& wR) {
   const T c = at(r), m = at(rho(r - 1)), p = at(rho(r + 1));
   const T a = c - m, b = p - c;
   T s;
@@ -39,13 +39,13 @@ __device__ __forceinline__ void recon_plm(const A& at, const Clamp& rho, int r, 
 }
 
 // 4th-order face value at x+1/2 (ppm.py:38)
-template <typename T, class A> __device__ __forceinline__ T ppm_face(const A& at, const Clamp& rho, int x) {
+template <typename T, class A, class RH> __device__ __forceinline__ T ppm_face(const A& at, const RH& rho, int x) {
   return T(7.0 / 12.0) * (at(x) + at(rho(x + 1))) - T(1.0 / 12.0) * (at(rho(x - 1)) + at(rho(x + 2)));
 }
-template <typename T, class A> __device__ __forceinline__ T ppm_d2c(const A& at, const Clamp& rho, int x) {
+template <typename T, class A, class RH> __device__ __forceinline__ T ppm_d2c(const A& at, const RH& rho, int x) {
   return (at(rho(x - 1)) - T(2) * at(x)) + at(rho(x + 1));
 }
-template <typename T, class A> __device__ __forceinline__ T ppm_d3(const A& at, const Clamp& rho, int x) {
+template <typename T, class A, class RH> __device__ __forceinline__ T ppm_d3(const A& at, const RH& rho, int x) {
   return ppm_d2c<T>(at, rho, rho(x + 1)) - ppm_d2c<T>(at, rho, x);
 }
 
@@ -54,8 +54,8 @@ template <typename T, class A> __device__ __forceinline__ T ppm_d3(const A& at, 
 // For finite data the limiter's no-extremum-anywhere branch
 // (limiters.py:141-143) gives the same values as the main branch, so the main
 // branch is evaluated for every cell.
-template <typename T, class A>
-__device__ __forceinline__ void recon_ppm(const A& at, const Clamp& rho, int r, T& wL, T& wR) {
+template <typename T, class A, class RH>
+__device__ __forceinline__ void recon_ppm(const A& at, const RH& rho, int r, T& wL, T& wR) {
   const T C = T(1.25);
   const T w0 = at(r), wm1 = at(rho(r - 1)), wp1 = at(rho(r + 1)), wm2 = at(rho(r - 2)), wp2 = at(rho(r + 2));
   const T fL = ppm_face<T>(at, rho, rho(r - 1));
@@ -91,8 +91,8 @@ __device__ __forceinline__ void recon_ppm(const A& at, const Clamp& rho, int r, 
 }
 
 // WENO-JS, eps = 1e-6 (weno.py:22-149)
-template <typename T, class A>
-__device__ __forceinline__ void recon_weno3(const A& at, const Clamp& rho, int r, T& wL, T& wR) {
+template <typename T, class A, class RH>
+__device__ __forceinline__ void recon_weno3(const A& at, const RH& rho, int r, T& wL, T& wR) {
   const T eps = T(1e-6);
   const T z = at(r), m1 = at(rho(r - 1)), p1 = at(rho(r + 1));
   const T g0 = T(1.0 / 3.0), g1 = T(2.0 / 3.0);
@@ -103,8 +103,8 @@ __device__ __forceinline__ void recon_weno3(const A& at, const Clamp& rho, int r
   wL = (a1g0 / (a0g1 + a1g0)) * (T(1.5) * z - T(.5) * p1) + (a0g1 / (a0g1 + a1g0)) * (T(.5) * z + T(.5) * m1);
 }
 
-template <typename T, class A>
-__device__ __forceinline__ void recon_weno5(const A& at, const Clamp& rho, int r, T& wL, T& wR) {
+template <typename T, class A, class RH>
+__device__ __forceinline__ void recon_weno5(const A& at, const RH& rho, int r, T& wL, T& wR) {
   const T eps = T(1e-6);
   const T z = at(r), m1 = at(rho(r - 1)), p1 = at(rho(r + 1)), m2 = at(rho(r - 2)), p2 = at(rho(r + 2));
   const T g0 = T(1.0 / 10.0), g1 = T(3.0 / 5.0), g2 = T(3.0 / 10.0);
@@ -132,8 +132,8 @@ __device__ __forceinline__ void recon_weno5(const A& at, const Clamp& rho, int r
   }
 }
 
-template <typename T, class A>
-__device__ __forceinline__ void recon_weno7(const A& at, const Clamp& rho, int r, T& wL, T& wR) {
+template <typename T, class A, class RH>
+__device__ __forceinline__ void recon_weno7(const A& at, const RH& rho, int r, T& wL, T& wR) {
   const T eps = T(1e-6);
   const T z = at(r), m1 = at(rho(r - 1)), p1 = at(rho(r + 1)), m2 = at(rho(r - 2)), p2 = at(rho(r + 2));
   const T m3 = at(rho(r - 3)), p3 = at(rho(r + 3));
@@ -173,8 +173,8 @@ __device__ __forceinline__ void recon_weno7(const A& at, const Clamp& rho, int r
   }
 }
 
-template <int SCH, typename T, class A>
-__device__ __forceinline__ void reconstruct(const A& at, const Clamp& rho, int r, int limiter, T& wL, T& wR) {
+template <int SCH, typename T, class A, class RH>
+__device__ __forceinline__ void reconstruct(const A& at, const RH& rho, int r, int limiter, T& wL, T& wR) {
   if constexpr (SCH == PCM) { wL = wR = at(r); }
   else if constexpr (SCH == PLM) recon_plm<T>(at, rho, r, limiter, wL, wR);
   else if constexpr (SCH == PPM) recon_ppm<T>(at, rho, r, wL, wR);

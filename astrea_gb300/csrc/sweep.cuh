@@ -18,6 +18,8 @@
 // access at virtual v of a level is served by the value at rho(v) (clamp for
 // outflow), which is the reference's per-intermediate np.pad.
 #pragma once
+#include <type_traits>
+
 #include "physics.cuh"
 #include "recon.cuh"
 
@@ -131,9 +133,9 @@ template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, un
 // One tile: cells [s0, s0+TS) along the sweep and rows [t0, t0+TT) across it.
 // Called by the single-grid kernel (one tile per CTA) and by the batched
 // persistent kernel (a work list of tiles of many grids).
-template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT>
-__device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, const int t0,
-                                           unsigned char* __restrict__ smem_raw) {
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, bool CL>
+__device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int s0, const int t0,
+                                                unsigned char* __restrict__ smem_raw) {
   using M = Model<MID>;
   using G = Geom<SCH, DIM, TS, TT>;
   using S = Smem<SCH, DIM, TS, TT, M::NV>;
@@ -149,8 +151,12 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
 
   const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
   const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
-  const Clamp rs_ = make_rho(a.bc, Ns);
-  const Clamp rt_ = make_rho(a.bc, Nt);
+  using Rho = typename std::conditional<CL, Clamp, NoClamp>::type;
+  Rho rs_, rt_;
+  if constexpr (CL) {
+    rs_ = make_rho(a.bc, Ns);
+    rt_ = make_rho(a.bc, Nt);
+  }
   const T gamma = a.gamma, gm1 = a.gm1;
   const int tid = threadIdx.x, nth = blockDim.x;
   // axis label of this sweep: its position in the step's iteration order
@@ -169,7 +175,8 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
       int row, col;
       if (DIM == 2 && AX == 0) { row = e % H; col = e / H; } else { col = e % W; row = e / W; }
       const int vs = s0 + G::Q_BEG + col, vt = t0 - G::QT + row;
-      const int gs = bc_map(vs, Ns, a.bc), gt = DIM == 2 ? bc_map(vt, Nt, a.bc) : 0;
+      const int gs = (vs >= 0 && vs < Ns) ? vs : bc_map(vs, Ns, a.bc);
+      const int gt = DIM == 2 ? ((vt >= 0 && vt < Nt) ? vt : bc_map(vt, Nt, a.bc)) : 0;
       const long long g = gidx(gs, gt);
       T q[8];
 #pragma unroll
@@ -470,8 +477,25 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
   }
 }
 
+// Clamping is only needed on outflow grids, for tiles whose widest level
+// (the staged state) reaches past the grid edge.
 template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT>
-__global__ void __launch_bounds__(256) sweep_kernel(const SweepArgs<T> a) {
+__device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, const int t0,
+                                           unsigned char* __restrict__ smem_raw) {
+  using G = Geom<SCH, DIM, TS, TT>;
+  const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
+  const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
+  const bool inside = s0 + G::Q_BEG >= 0 && s0 + TS + G::Q_END <= Ns &&
+                      (DIM == 1 || (t0 - G::QT >= 0 && t0 + TT + G::QT <= Nt));
+  if (a.bc == EDGE && !inside) sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, true>(a, s0, t0, smem_raw);
+  else sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false>(a, s0, t0, smem_raw);
+}
+
+// FP32 Euler tiles fit four CTAs per SM (<= 64 registers); FP64 and MHD tiles are larger
+template <typename T, int MID> struct SweepOcc { static constexpr int value = (sizeof(T) == 4 && MID != 8) ? 4 : 1; };
+
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT>
+__global__ void __launch_bounds__(256, SweepOcc<T, MID>::value) sweep_kernel(const SweepArgs<T> a) {
   if (a.clock->done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT>(a, blockIdx.x * TS, blockIdx.y * TT, smem_raw);

@@ -1,0 +1,260 @@
+"""Continuous-batching server for solve requests.
+
+A request is one independent simulation: an initial state (point
+primitives), a method (scheme x solver), and an end time.  The server keeps
+one slot batch per (dimension, variable model) class on the GPU.  Requests
+are admitted as soon as they have arrived *and* their class has a free slot
+and room in its arena; the device memory of all classes together is bounded
+by an HBM budget fixed at start-up.  Every iteration advances all admitted,
+unfinished requests of every class by a few of their own time steps (the
+classes run on separate CUDA streams, so their kernels overlap), then
+retires finished requests, frees their memory, and admits waiting ones.
+Latency = completion time - arrival time.
+
+The reference has no serving layer (one simulation per process,
+astrea.py:90-226); this is built on the batched engine.
+"""
+
+import bisect
+import math
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .batch import SlotBatch
+from .solver import RunConfig
+
+# bytes of device memory one state element costs in a class: the caller-side state
+# and primitive arenas plus the engine's two stage and two divergence buffers and one scratch
+ARENA_COPIES = 7
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float
+    dim: int
+    n: int
+    mhd: bool
+    scheme: str
+    solver: str
+    t_end: float
+    seed: int
+    boundary: str = "edge"
+    gamma: float = 1.4
+    cfl: float = 0.8
+    compat: bool = False
+    # filled in by the server
+    admitted: float = math.nan
+    finished: float = math.nan
+    steps: int = 0
+    status: int = 0
+    result: object = None
+
+    @property
+    def model(self):
+        return 8 if self.mhd else (3 if self.dim == 1 else 4)
+
+    @property
+    def cells(self):
+        return self.n * (self.n if self.dim == 2 else 1)
+
+    def config(self, precision):
+        return RunConfig(dim=self.dim, n0=self.n, n1=self.n if self.dim == 2 else 1, model=self.model,
+                         precision=precision, scheme=self.scheme, solver=self.solver, integrator="ssprk33",
+                         boundary=self.boundary, gamma=self.gamma, dx=1.0 / self.n, cfl=self.cfl, t_end=self.t_end,
+                         compat=self.compat)
+
+    def initial_state(self):
+        """Point primitives: seeded Riemann data (two states in 1D, four quadrants in 2D)."""
+        rng = np.random.default_rng(self.seed)
+
+        def state():
+            s = np.zeros(8)
+            s[0], s[4] = rng.uniform(.1, 2), rng.uniform(.1, 2)
+            s[1:4] = rng.uniform(-1, 1, 3) if self.mhd else [rng.uniform(-1, 1), 0 if self.dim == 1 else
+                                                              rng.uniform(-1, 1), 0]
+            if self.mhd:
+                s[5:8] = rng.uniform(-1, 1, 3)
+            return s
+
+        n = self.n
+        if self.dim == 1:
+            w = np.zeros((n, 8))
+            w[: n // 2], w[n // 2:] = state(), state()
+        else:
+            w = np.zeros((n, n, 8))
+            h = n // 2
+            w[:h, :h], w[:h, h:], w[h:, :h], w[h:, h:] = state(), state(), state(), state()
+        return w
+
+
+def make_requests(count, rate, seed=20261203, n1d=(256, 65536), n2d=(128, 2048), frac_1d=0.4, frac_mhd=0.5,
+                  t_end=(0.05, 0.3)):
+    """Seeded request stream: Poisson arrivals at ``rate``/s, the mixed sizes and methods of the serving workload."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(count):
+        t += rng.exponential(1.0 / rate)
+        dim = 1 if rng.uniform() < frac_1d else 2
+        lo, hi = n1d if dim == 1 else n2d
+        n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        n = max(8, n - n % 2)
+        mhd = bool(rng.uniform() < frac_mhd)
+        scheme = ["plm", "ppm", "weno5"][rng.integers(3)]
+        solver = ["llf", "hlld" if mhd else "hllc"][rng.integers(2)]
+        out.append(Request(rid=i, arrival=t, dim=dim, n=n, mhd=mhd, scheme=scheme, solver=solver,
+                           t_end=float(rng.uniform(*t_end)), seed=int(rng.integers(1 << 31))))
+    return out
+
+
+class Arena:
+    """First-fit allocator of element ranges."""
+
+    def __init__(self, capacity):
+        self.capacity = capacity
+        self.free = [(0, capacity)]  # sorted (start, size)
+
+    def alloc(self, size):
+        for i, (s, n) in enumerate(self.free):
+            if n >= size:
+                if n == size:
+                    self.free.pop(i)
+                else:
+                    self.free[i] = (s + size, n - size)
+                return s
+        return None
+
+    def release(self, start, size):
+        i = bisect.bisect(self.free, (start, size))
+        self.free.insert(i, (start, size))
+        merged = []
+        for s, n in self.free:
+            if merged and merged[-1][0] + merged[-1][1] == s:
+                merged[-1] = (merged[-1][0], merged[-1][1] + n)
+            else:
+                merged.append((s, n))
+        self.free = merged
+
+
+@dataclass
+class ServeStats:
+    latencies_ms: list = field(default_factory=list)
+    cell_updates: float = 0.0
+    wall_s: float = 0.0
+    failed: int = 0
+    max_active: int = 0
+
+    def summary(self):
+        lat = np.array(self.latencies_ms) if self.latencies_ms else np.array([math.nan])
+        return {"requests": len(self.latencies_ms), "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "cell_updates_per_s": self.cell_updates / max(self.wall_s, 1e-9),
+                "wall_s": self.wall_s, "non_finite": self.failed, "max_active": self.max_active}
+
+
+class Server:
+    """Continuous batching of solve requests under an HBM budget."""
+
+    CLASSES = ((1, 3), (1, 8), (2, 4), (2, 8))
+
+    def __init__(self, hbm_budget_bytes=150e9, precision=32, max_slots=256, shares=None, keep_results=False,
+                 steps_per_poll=4, device=None):
+        self.precision = precision
+        esize = 4 if precision == 32 else 8
+        shares = shares or {(1, 3): .1, (1, 8): .1, (2, 4): .5, (2, 8): .3}
+        self.device = torch.device(device or "cuda")
+        self.batches, self.arenas, self.streams, self.free_slots = {}, {}, {}, {}
+        self.classes = []
+        for cls in self.CLASSES:
+            cap = int(hbm_budget_bytes * shares.get(cls, 0) / (ARENA_COPIES * esize))
+            cap -= cap % 8
+            if cap <= 0:
+                continue
+            self.classes.append(cls)
+            self.batches[cls] = SlotBatch(cls[0], cls[1], precision, "ssprk33", max_slots, cap, self.device)
+            self.arenas[cls] = Arena(cap)
+            self.streams[cls] = torch.cuda.Stream(self.device)
+            self.free_slots[cls] = list(range(max_slots))[::-1]
+        self.keep_results = keep_results
+        self.steps_per_poll = steps_per_poll
+
+    def _admit(self, r, now):
+        cls = (r.dim, r.model)
+        size = r.model * r.cells
+        if not self.free_slots[cls]:
+            return False
+        off = self.arenas[cls].alloc(size)
+        if off is None:
+            return False
+        slot = self.free_slots[cls].pop()
+        with torch.cuda.stream(self.streams[cls]):
+            self.batches[cls].occupy(slot, r.config(self.precision), off, r.initial_state())
+        r.admitted = now
+        self.active[cls][slot] = (r, off, size)
+        return True
+
+    def serve(self, requests, realtime=True, max_wall_s=None):
+        """Run the request stream; returns ServeStats (requests are updated in place)."""
+        stats = ServeStats()
+        pending = {cls: deque() for cls in self.classes}
+        for r in sorted(requests, key=lambda x: x.arrival):
+            cls = (r.dim, r.model)
+            if cls not in pending:
+                raise ValueError(f"request {r.rid}: no device memory was budgeted for class {cls}")
+            size = r.model * r.cells
+            if size > self.arenas[cls].capacity:
+                raise ValueError(f"request {r.rid} ({size} elements) exceeds its class arena")
+            pending[cls].append(r)
+        self.active = {cls: {} for cls in self.classes}
+        t0 = time.perf_counter()
+        while any(pending.values()) or any(self.active.values()):
+            now = time.perf_counter() - t0
+            if max_wall_s is not None and now > max_wall_s:
+                break
+            for cls in self.classes:
+                q = pending[cls]
+                while q and (q[0].arrival <= now or not realtime):
+                    if not self._admit(q[0], now):
+                        break
+                    q.popleft()
+            n_active = sum(len(a) for a in self.active.values())
+            stats.max_active = max(stats.max_active, n_active)
+            if n_active == 0:
+                nxt = min((q[0].arrival for q in pending.values() if q), default=None)
+                if nxt is not None and realtime:
+                    time.sleep(max(0.0, min(nxt - now, 0.05)))
+                continue
+            for cls in self.classes:
+                if self.active[cls]:
+                    with torch.cuda.stream(self.streams[cls]):
+                        self.batches[cls].step(self.steps_per_poll)
+            for cls in self.classes:
+                if not self.active[cls]:
+                    continue
+                with torch.cuda.stream(self.streams[cls]):
+                    clk = self.batches[cls].clocks()
+                now = time.perf_counter() - t0
+                for slot in list(self.active[cls].keys()):
+                    if not clk["done"][slot]:
+                        continue
+                    r, off, size = self.active[cls].pop(slot)
+                    r.finished = now
+                    r.steps = int(clk["steps"][slot])
+                    r.status = int(clk["status"][slot])
+                    if r.status:
+                        stats.failed += 1
+                    stats.cell_updates += r.cells * r.steps
+                    stats.latencies_ms.append(1e3 * (r.finished - r.arrival))
+                    if self.keep_results:
+                        with torch.cuda.stream(self.streams[cls]):
+                            r.result = self.batches[cls].planes(slot).clone()
+                    self.batches[cls].release(slot)
+                    self.arenas[cls].release(off, size)
+                    self.free_slots[cls].append(slot)
+        torch.cuda.synchronize(self.device)
+        stats.wall_s = time.perf_counter() - t0
+        return stats

@@ -1,25 +1,30 @@
 #!/usr/bin/env python3
 """Benchmark of the per-step finite-volume update on GB300.
 
-Workload (the headline configuration): 2D Euler shear layer, gamma = 1.4,
-2048 x 2048 periodic cells on [0,1]^2, rho = 2 and v_x = +0.5 for
-|y - 0.5| < 0.25, rho = 1 and v_x = -0.5 elsewhere, p = 2.5, v_y =
-0.01 sin(4 pi x) + seeded uniform noise of amplitude 1e-3; PPM (McCorquodale-
-Colella limiter) + HLLC + SSPRK3 at CFL 0.8.  One step = one full SSPRK3 step
-(three stages) of the whole grid.  Synthetic data (seeded), no dataset.
+Headline workload: 2D Euler shear layer, gamma = 1.4, 2048 x 2048 periodic
+cells on [0,1]^2; rho = 2 and v_x = +0.5 for |y - 0.5| < 0.25, rho = 1 and
+v_x = -0.5 elsewhere, p = 2.5, v_y = 0.01 sin(4 pi x) + seeded uniform noise of
+amplitude 1e-3; PPM (McCorquodale-Colella limiter) + HLLC + SSPRK3 at CFL 0.8.
+One step = one full SSPRK3 step (three stages) of the whole grid.  Seeded
+synthetic data; no dataset is involved.
 
-Arms:
-  default             our CUDA path; value = FP32 cell-updates/s with the state
-                      resident in HBM; also the plain FP64 rate, the FP32-vs-FP64
-                      L1(rho) error, the end-to-end rate through the C ABI with
-                      host buffers, the roofline of the sweep kernel and a CPU
-                      baseline (the oracle on a bounded sample).
-  --impl reference    the reference's algorithm on the host CPU cores (the
-                      oracle restatement, one process per core on independent
-                      bounded samples of the same workload).
+Legs of the default arm (all numbers in cell-updates/s):
+  value        FP32 (FP64 pressure recovery), state resident in HBM
+  fp64_plain   the plain all-FP64 path on the same workload
+  l1_rho       L1(rho) of FP32 against FP64 after the same steps
+  e2e          through the C ABI with the state copied host->device and
+               device->host (pinned) every step
+  batched      512 independent four-quadrant Riemann grids, 128^2..1024^2,
+               PLM+LLF / PPM+HLLC 50/50, FP32, one persistent kernel per sweep
+  serving      continuous batching of a seeded Poisson request stream
+               (sizes scaled down 4x per axis from the full request mix so the
+               leg takes seconds; see --serve-*)
+  cpu_baseline the oracle (NumPy restatement of the reference) on one core,
+               SSPRK3 steps of a 256^2 instance of the headline workload
+--impl reference: the reference's algorithm (the oracle) on all host cores,
+independent 256^2 instances, one process per core.
 
-Multi-GPU (torchrun): independent replicas, no collective (the batched and
-single-grid workloads do not exchange data); value sums all ranks.
+Multi-GPU (torchrun): independent replicas, no collective; value sums ranks.
 """
 
 import argparse
@@ -40,6 +45,9 @@ sys.path.insert(0, ROOT)
 SEED = 20261203
 METRIC = "cell-updates/s FP32-batched vs FP64 plain (L1<=1e-5); serve p50/p99 ms"
 WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc)+HLLC+SSPRK3, CFL 0.8"
+# DRAM bytes (read + write) of one stage-0 sweep launch of the headline FP32
+# workload, measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum)
+SWEEP_DRAM_BYTES = 103.7e6
 
 
 def shear_layer(n, seed=SEED):
@@ -80,10 +88,11 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            time.sleep(0.3)
         except Exception:
             self.proc = None
         return self
@@ -101,7 +110,7 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        sm, mx, power, reasons = [], None, [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
@@ -110,13 +119,14 @@ class ClockSampler:
             try:
                 sm.append(float(f[1]))
                 mx = float(f[2])
+                power.append(float(f[3]))
             except ValueError:
                 continue
             for name, v in zip(names, f[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w_max": max(power) if power else None}
 
 
 def measured_peaks():
@@ -129,32 +139,34 @@ def measured_peaks():
 
 
 def cpu_sample_worker(args):
-    """One bounded CPU sample: one SSPRK3 step of an n x n shear layer with the oracle."""
-    n, seed = args
+    """One bounded CPU sample: ``steps`` SSPRK3 steps of an n x n shear layer with the oracle."""
+    n, seed, steps = args
     import numpy as np_
     sys.path.insert(0, ROOT)
     from oracle import stepper
     cfg = stepper.OracleConfig(dim=2, scheme="ppm", solver="hllc", integrator="ssprk33", gamma=1.4, bc="wrap",
-                               dx=1.0 / n, cfl=0.8, eig="analytic", t_end=1.0)
+                               dx=1.0 / n, cfl=0.8, eig="analytic", t_end=1.0, compat=False)
     q = stepper.initialise(shear_layer(n, seed), cfg)
+    t, idx, order = 0.0, 1, [0, 1]
     t0 = time.perf_counter()
     with np_.errstate(all="ignore"):
-        stepper.step(q, cfg, 0.0, 1, [0, 1])
+        for _ in range(steps):
+            q, t, idx, order, _dt = stepper.step(q, cfg, t, idx, order)
     return time.perf_counter() - t0
 
 
-def cpu_baseline(n=256, procs=1):
+def cpu_baseline(n=256, procs=1, steps=1):
     """Oracle (NumPy restatement of the reference) on host cores: cell-updates/s."""
     if procs <= 1:
-        dt = cpu_sample_worker((n, SEED))
-        return n * n / dt, 1
+        dt = cpu_sample_worker((n, SEED, steps))
+        return n * n * steps / dt, 1
     import multiprocessing as mp
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
         t0 = time.perf_counter()
-        pool.map(cpu_sample_worker, [(n, SEED + i) for i in range(procs)])
+        pool.map(cpu_sample_worker, [(n, SEED + i, steps) for i in range(procs)])
         wall = time.perf_counter() - t0
-    return procs * n * n / wall, procs
+    return procs * n * n * steps / wall, procs
 
 
 def dist_init():
@@ -190,35 +202,90 @@ def reference_arm(args):
     procs = max(1, len(os.sched_getaffinity(0)))
     n = args.cpu_n
     for _ in range(args.warmup):
-        cpu_sample_worker((32, SEED))
+        cpu_sample_worker((32, SEED, 1))
     vals = []
     for _ in range(args.steps):
-        v, _p = cpu_baseline(n, procs)
+        v, _p = cpu_baseline(n, procs, 1)
         vals.append(v)
     value = statistics.median(vals)
+    sample = f"{procs} processes, each one SSPRK3 step of an independent {n}^2 instance, oracle (NumPy restatement)"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n * n * procs / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": f"{procs} processes x one SSPRK3 step of a {n}^2 instance"},
-            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": procs, "kind": "port",
-                             "sample": f"{procs} independent {n}^2 instances, one step each, oracle (NumPy restatement)"},
+            "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": procs, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
+def batched_leg(steps, warmup, ngrids=512, seed=SEED):
+    """512 four-quadrant Riemann grids, sides 2^k (k in 7..10), PLM+LLF / PPM+HLLC 50/50, FP32."""
+    import torch
+    from astrea_gb300.batch import Batch
+    from astrea_gb300.solver import RunConfig
+    from astrea_gb300.serving import Request
+    rng = np.random.default_rng(seed)
+    cfgs, ws = [], []
+    for g in range(ngrids):
+        n = 2 ** int(rng.integers(7, 11))
+        ppm = bool(rng.uniform() < .5)
+        cfgs.append(RunConfig(dim=2, n0=n, n1=n, model=4, precision=32, scheme="ppm" if ppm else "plm",
+                              solver="hllc" if ppm else "llf", integrator="ssprk33", boundary="edge", gamma=1.4,
+                              dx=1.0 / n, cfl=0.8, t_end=0.25, compat=False))
+        ws.append(Request(rid=g, arrival=0.0, dim=2, n=n, mhd=False, scheme="plm", solver="llf", t_end=.25,
+                          seed=int(rng.integers(1 << 31))).initial_state())
+    b = Batch(cfgs)
+    b.initialise(ws)
+    del ws
+    cells = sum(c.n0 * c.n1 for c in cfgs)
+    b.step(warmup, graph=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c_before = b.clocks()["steps"].copy()
+    e0.record()
+    b.step(steps, graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = b.clocks()
+    done_updates = float(sum((clk["steps"][g] - c_before[g]) * cfgs[g].n0 * cfgs[g].n1 for g in range(ngrids)))
+    return {"value": done_updates / (ms / 1e3), "unit": "cell-updates/s", "grids": ngrids, "cells": cells,
+            "steps": steps, "ms_per_step": ms / steps, "non_finite_grids": int((clk["status"] != 0).sum()),
+            "workload": "512 four-quadrant Riemann grids 128^2..1024^2, PLM+LLF/PPM+HLLC 50/50, FP32, edge, CFL 0.8",
+            "graph": "one CUDA graph per step, persistent sweep kernels over a tile work list"}
+
+
+def serving_leg(count, rate, seed=SEED):
+    from astrea_gb300.serving import Server, make_requests
+    reqs = make_requests(count, rate, seed=seed, n1d=(64, 16384), n2d=(32, 512))
+    srv = Server(hbm_budget_bytes=150e9, precision=32, max_slots=256, steps_per_poll=4)
+    stats = srv.serve(reqs)
+    out = stats.summary()
+    out.update({"rate_per_s": rate, "mix": "40% 1D N log-U[64,16384], 60% 2D side log-U[32,512] (full mix / 4 per "
+                                         "axis), Euler|MHD 50/50, {PLM,PPM,WENO5}x{LLF,HLLC|HLLD}, t_end U[.05,.3]",
+                "hbm_budget_gb": 150})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=2048)
-    ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--cpu-n", type=int, default=192)
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--serve-requests", type=int, default=120)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--cpu-n", type=int, default=256)
+    ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving legs")
     ap.add_argument("--only-fp32", action="store_true",
-                    help="time the FP32 path only (no FP64, e2e or CPU legs); used for profiler captures")
+                    help="time the FP32 path only (no FP64, e2e, batched, serving or CPU legs); for profiler captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -230,8 +297,9 @@ def main():
     from astrea_gb300.solver import Solver
     n = args.n
     w0 = shear_layer(n)
+    cells = n * n
 
-    # ---- FP32 (headline), state resident in HBM
+    # ---- FP32 (headline), state resident in HBM; events around every launch
     s32 = Solver(run_config(n, 32))
     s32.initialise(w0)
     s32.reset_clock()
@@ -249,24 +317,27 @@ def main():
                                              kernel_ms, launches, ctypes.c_void_p(stream.cuda_stream)))
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = allmax(e0.elapsed_time(e1), ws)
     barrier(ws)
-    ms = allmax(ms, ws)
-    cells = n * n
     value = ws * cells * args.steps / (ms / 1e3)
     clk32 = s32.clock()
 
-    # ---- roofline of the sweep kernel: algorithmic bytes per launch / mean launch time
+    # roofline of the sweep kernel: algorithmic bytes per launch / mean launch time.
+    # Per step: stage 0 two sweeps read the state and write a divergence (2*C*s per cell each);
+    # stages 1-2: the first sweep the same, the second reads state, divergence and u0 and writes
+    # the stage result (4*C*s).  C = 4 stored variables, s = 4 bytes.
     C, sz = 4, 4
-    # per step: 3 stages x (first sweep: read state + write divergence = 2*C*s per cell;
-    # second sweep: stage 0 the same, stages 1-2 read state, divergence, u0 and write the result = 4*C*s)
     alg_bytes_step = cells * C * sz * (2 + 2 + (2 + 4) + (2 + 4))
-    sweep_launches = launches[0]
-    sweep_ms = kernel_ms[0]
-    alg_per_launch = alg_bytes_step * args.steps / max(sweep_launches, 1)
-    achieved = alg_per_launch / (sweep_ms / max(sweep_launches, 1) / 1e3) / 1e9
+    sweep_launches = max(launches[0], 1)
+    alg_per_launch = alg_bytes_step * args.steps / sweep_launches
+    achieved = alg_per_launch / (kernel_ms[0] / sweep_launches / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
-    step_alg = cells * 8 * C * sz  # 8 state passes per SSPRK3 step (minimum traffic)
+    step_alg = cells * 8 * C * sz  # 8 state passes per SSPRK3 step: the minimum traffic
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": SWEEP_DRAM_BYTES * (alg_per_launch / (2 * cells * C * sz)),
+                "kernel": "sweep_kernel (every sweep launch of the timed steps)", "peak_source": peak_kind,
+                "alg_bytes_per_launch": alg_per_launch, "step_frac": step_alg * (value / ws) / cells / 1e9 / peak,
+                "note": "ALU/issue-bound stencil: thousands of FP32 ops per cell-update against 128 B"}
 
     if args.only_fp32:
         if rank == 0:
@@ -274,11 +345,10 @@ def main():
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                               "config": {"workload": WORKLOAD, "cells": cells}, "only_fp32": True,
                               "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1],
-                                            "bookkeeping": kernel_ms[2]}, "roofline_achieved_gbs": achieved}),
-                  flush=True)
+                                            "bookkeeping": kernel_ms[2]}, "roofline": roofline}), flush=True)
         return 0
 
-    # ---- FP64 plain, same workload, and L1(rho) of FP32 against it after the same steps
+    # ---- FP64 plain, same workload
     s64 = Solver(run_config(n, 64))
     s64.initialise(w0)
     s64.reset_clock()
@@ -291,15 +361,14 @@ def main():
     torch.cuda.synchronize()
     ms64 = f0.elapsed_time(f1)
     value64 = cells * args.fp64_steps / (ms64 / 1e3)
-    # L1(rho) after the same number of steps from the same initial state
+    # L1(rho) of FP32 against FP64 after the same number of steps from the same initial state
     k = args.fp64_steps + 1
     a32 = Solver(run_config(n, 32))
     a32.initialise(w0)
     a32.reset_clock()
     a32.step(k)
-    rho32 = a32.state[0].double()
-    rho64 = s64.state[0]
-    l1 = float(torch.mean(torch.abs(rho32 - rho64)).item())
+    l1 = float(torch.mean(torch.abs(a32.state[0].double() - s64.state[0])).item())
+    del a32, s64
 
     # ---- end to end through the C ABI with host buffers (pinned): H2D state, one step, D2H state
     host = torch.empty_like(s32.state, device="cpu").pin_memory()
@@ -311,44 +380,52 @@ def main():
     torch.cuda.synchronize()
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     g0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(args.e2e_steps):
         s32.state.copy_(host, non_blocking=True)
         s32.step(1, graph=True)
         host.copy_(s32.state, non_blocking=True)
     g1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = allmax(g0.elapsed_time(g1), ws)
-    e2e = ws * cells * args.steps / (e2e_ms / 1e3)
+    e2e = ws * cells * args.e2e_steps / (e2e_ms / 1e3)
     state_bytes = s32.state.numel() * s32.state.element_size()
+    del s32
+    torch.cuda.empty_cache()
+
+    batched = serving = None
+    if not args.no_extras:
+        batched = batched_leg(args.batch_steps, 2)
+        torch.cuda.empty_cache()
+        serving = serving_leg(args.serve_requests, args.serve_rate)
+        torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, cores = cpu_baseline(args.cpu_n, 1)
+        v, cores = cpu_baseline(args.cpu_n, 1, args.cpu_steps)
         cpu = {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-               "sample": f"one SSPRK3 step of a {args.cpu_n}^2 instance of the workload, oracle (NumPy), 1 core"}
+               "sample": f"{args.cpu_steps} SSPRK3 steps of a {args.cpu_n}^2 instance of the workload, "
+                         f"oracle (NumPy restatement of the reference), 1 core"}
 
     if rank == 0:
-        per_step_launches = (launches[0] + launches[1] + launches[2]) / args.steps
         line = {
             "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "cells": cells, "precision": "fp32 (FP64 pressure recovery)",
-                       "hllc": "textbook (flag PHYSICAL)",
-                       "parallelism": f"replicas x{ws}", "l2": "working set 5 x 67 MB > L2 (inputs larger than L2)"},
+                       "hllc": "textbook (flag PHYSICAL)", "parallelism": f"replicas x{ws}",
+                       "l2": "working set 5 x 67 MB > L2: inputs larger than L2"},
             "fp64_plain": {"value": value64, "unit": "cell-updates/s", "steps": args.fp64_steps,
                            "ms_per_step": ms64 / args.fp64_steps},
             "fp32_over_fp64": value / ws / value64,
             "l1_rho_fp32_vs_fp64": l1, "l1_after_steps": k,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "sweep_kernel (all sweep launches)",
-                         "peak_source": peak_kind,
-                         "step_frac": step_alg * (value / ws) / cells / 1e9 / peak},
+            "roofline": roofline,
             "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1], "bookkeeping": kernel_ms[2]},
             "gpu_launches": launches[0] + launches[1] + launches[2],
-            "launches_per_step": per_step_launches,
+            "launches_per_step": (launches[0] + launches[1] + launches[2]) / args.steps,
             "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
-                    "d2h_bytes_per_step": state_bytes},
+                    "d2h_bytes_per_step": state_bytes, "steps": args.e2e_steps},
+            "batched": batched,
+            "serving": serving,
             "clocks": cs.summary(),
             "cpu_baseline": cpu,
             "t_simulated": clk32["t"],

@@ -31,9 +31,15 @@ def test_mix_equals_alone():
         s.reset_clock()
         clk = s.run()
         assert clk["steps"] == r.steps, r
+        assert bool(clk["status"]) == bool(r.status), r
         a, b = r.result.double(), s.state.double()
-        err = float(torch.max(torch.abs(a - b)) / torch.max(torch.abs(b)))
-        assert err <= 1e-6, (r, err)
+        # some random MHD Riemann problems lose positivity (the FP64 oracle goes
+        # non-finite on them too): the non-finite pattern must match as well
+        fa, fb = torch.isfinite(a), torch.isfinite(b)
+        assert torch.equal(fa, fb), r
+        if fb.any():
+            err = float(torch.max(torch.abs(a[fb] - b[fb])) / torch.max(torch.abs(b[fb])))
+            assert err <= 1e-6, (r, err)
 
 
 def test_admission_respects_the_memory_budget():

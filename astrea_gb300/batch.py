@@ -150,18 +150,22 @@ class Batch:
     def planes(self, g):
         return self.sb.planes(g)
 
+    def initialise_one(self, g, w):
+        """Point primitives (n0[, n1], 8) of grid g (NumPy or torch, host or device) -> its averages."""
+        cfg, off = self.sb.slots[g]
+        t = torch.as_tensor(w)
+        if t.dim() == 2:
+            t = t[:, None, :]
+        n = self.nv * t.shape[0] * t.shape[1]
+        self.sb.prim_arena[off:off + n].view(self.nv, t.shape[0], t.shape[1]).copy_(
+            t[..., MODEL_VARS[self.model]].permute(2, 0, 1).to(self.arena.dtype))
+        _lib.check(self.sb.lib.astrea_batch_initialise(self.sb.handle, g,
+                                                       ctypes.c_void_p(self.sb.prim_arena.data_ptr()),
+                                                       ctypes.c_void_p(self.arena.data_ptr()), _stream()))
+
     def initialise(self, prims):
         for g, w in enumerate(prims):
-            cfg, off = self.sb.slots[g]
-            t = torch.as_tensor(w)
-            if t.dim() == 2:
-                t = t[:, None, :]
-            n = self.nv * t.shape[0] * t.shape[1]
-            self.sb.prim_arena[off:off + n].view(self.nv, t.shape[0], t.shape[1]).copy_(
-                t[..., MODEL_VARS[self.model]].permute(2, 0, 1).to(self.arena.dtype))
-            _lib.check(self.sb.lib.astrea_batch_initialise(self.sb.handle, g,
-                                                           ctypes.c_void_p(self.sb.prim_arena.data_ptr()),
-                                                           ctypes.c_void_p(self.arena.data_ptr()), _stream()))
+            self.initialise_one(g, w)
         torch.cuda.current_stream().synchronize()
 
     def step(self, n=1, graph=True):

@@ -44,8 +44,11 @@ static __global__ void dt_kernel(Clock* clocks, int ngrids) {
     dt = c.chkpt * c.idx - c.t;
     c.idx += 1;
   }
-  if (!(dt == dt)) c.status |= 1;
   c.dt = dt;
+  // A NaN speed gives a NaN dt; an infinite speed (vacuum) gives dt = 0, on which
+  // the reference's loop would never reach t_end.  Either way the grid is flagged
+  // and stopped (the rest of this step runs, then end_step marks it done).
+  if (!(dt > 0.0) || isinf(dt)) c.status |= 1;
 }
 
 // After the last stage: advance t, count the step, flip the axis order
@@ -61,7 +64,7 @@ static __global__ void end_step_kernel(Clock* clocks, int ngrids) {
   if (c.naxes == 2) c.order ^= 1;
   c.emax[0] = 0ull;
   c.emax[1] = 0ull;
-  if (!(c.t < c.t_end)) c.done = 1;
+  if (!(c.t < c.t_end) || (c.status & 1)) c.done = 1;
 }
 
 // index helpers in the physical frame: axis 0 (x, stride n1), axis 1 (y, contiguous)

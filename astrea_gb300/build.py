@@ -70,6 +70,8 @@ def build(jobs=None, force=False, verbose=False):
         objs.append(obj)
         if force or not os.path.exists(obj):
             cmds.append((src, [nv] + fl + ["-c", cu, "-o", obj]))
+    # longest units first (batched kernels, then the high-order sweeps) so the pool drains evenly
+    cmds.sort(key=lambda c: (not c[0].startswith("batch_k"), not c[0].startswith(("sweep_f64", "sweep_f32_w")), c[0]))
     jobs = jobs or max(1, min(len(cmds), os.cpu_count() or 4))
     if cmds:
         with cf.ThreadPoolExecutor(max_workers=jobs) as ex:

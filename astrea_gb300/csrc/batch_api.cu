@@ -17,10 +17,8 @@
 using namespace astrea;
 
 namespace astrea {
-ASTREA_EXTERN_BATCH(float, 1)
-ASTREA_EXTERN_BATCH(float, 2)
-ASTREA_EXTERN_BATCH(double, 1)
-ASTREA_EXTERN_BATCH(double, 2)
+ASTREA_EXTERN_BATCH(float)
+ASTREA_EXTERN_BATCH(double)
 }  // namespace astrea
 
 template <typename T> static BatchFn<T> batched_for(int model, int dim, int ax) {

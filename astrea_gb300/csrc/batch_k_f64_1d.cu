@@ -1,6 +1,6 @@
-// Batched sweep kernels for precision double, 1D.
+// Batched sweep kernels: double, 1D, model 3 axis 0, model 8 axis 0.
 #include "batch_launch.cuh"
 namespace astrea {
-template BatchFn<double> get_batched<double, 1>(int, int);
-template int get_occupancy<double, 1>(int, int);
+ASTREA_BATCH_INST(double, 3, 1, 0)
+ASTREA_BATCH_INST(double, 8, 1, 0)
 }

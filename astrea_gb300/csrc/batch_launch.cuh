@@ -1,5 +1,7 @@
-// Launchers of the batched persistent sweep kernel; each batch_k_<prec>_<dim>d.cu
-// translation unit instantiates the getters for one (precision, dimension).
+// Launchers of the batched persistent sweep kernel.  Each batch_k_*.cu
+// translation unit instantiates the launchers of one (precision, model, axis)
+// so that the large kernels compile in parallel; batch_api.cu only takes
+// their addresses.
 #pragma once
 #include "batch.cuh"
 
@@ -47,8 +49,20 @@ template <typename T, int DIM> int get_occupancy(int model, int ax) {
   }
 }
 
-#define ASTREA_EXTERN_BATCH(T, D)                                  \
-  extern template BatchFn<T> get_batched<T, D>(int, int);          \
-  extern template int get_occupancy<T, D>(int, int);
+#define ASTREA_BATCH_INST(T, MID, DIM, AX)                                                   \
+  template cudaError_t launch_batched<T, MID, DIM, AX>(const BatchArgs<T>&, int, cudaStream_t); \
+  template int occupancy<T, MID, DIM, AX>();
+
+#define ASTREA_BATCH_EXTERN(T, MID, DIM, AX)                                                        \
+  extern template cudaError_t launch_batched<T, MID, DIM, AX>(const BatchArgs<T>&, int, cudaStream_t); \
+  extern template int occupancy<T, MID, DIM, AX>();
+
+#define ASTREA_EXTERN_BATCH(T)        \
+  ASTREA_BATCH_EXTERN(T, 3, 1, 0)     \
+  ASTREA_BATCH_EXTERN(T, 8, 1, 0)     \
+  ASTREA_BATCH_EXTERN(T, 4, 2, 0)     \
+  ASTREA_BATCH_EXTERN(T, 4, 2, 1)     \
+  ASTREA_BATCH_EXTERN(T, 8, 2, 0)     \
+  ASTREA_BATCH_EXTERN(T, 8, 2, 1)
 
 }  // namespace astrea

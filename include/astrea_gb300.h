@@ -144,6 +144,30 @@ int astrea_to_primitive(astrea_handle* h, const void* state, void* prim_out, voi
  * the host).  sums_host receives nv doubles.  Synchronises ``stream``. */
 int astrea_reduce_conserved(astrea_handle* h, const void* state, double* sums_host, void* stream);
 
+/* The same sums without a handle and without allocating anything.  This entry
+ * point has no counterpart in the reference (which sums with NumPy on the
+ * host).  It is for callers that hold only a state pointer and must not
+ * allocate device memory at that moment: a grid inside a batched arena in a
+ * process whose HBM is fully budgeted to its arenas, or a monitor reporting
+ * totals while the device is out of memory.  A handle would allocate the full
+ * set of stage buffers of the grid just to sum it.
+ *
+ * state: nv planes of ``cells`` elements each (float if precision == 32, double
+ * if 64), on the current device.  The partial sums live in a fixed device array
+ * of 2440 doubles (19,520 bytes) per device: 152 blocks x up to 8 variables x
+ * (sum, compensation), plus the 8 folded sums.  nv above 8 (or below 1) is
+ * rejected with ASTREA_ERR_ARG.  Nothing in that array needs to start at zero:
+ * every partial is written before it is read.  The results equal
+ * astrea_reduce_conserved's on the same state (same blocks, same order).
+ *
+ * The first call on each device, made with that device current, looks up the
+ * array's address (cudaGetSymbolAddress); make that first call before any
+ * stream capture begins.  There is one array per device, so calls that overlap
+ * on the same device (from other threads or on other streams) race on it and
+ * give wrong sums: serialise them.  Synchronises ``stream``. */
+int astrea_reduce_conserved_static(const void* state, int precision, long long cells, int nv, double* sums_host,
+                                   void* stream);
+
 /* ------------------------------------------------------------------------
  * Batched engine: many independent grids of uneven sizes in one state arena.
  * The reference runs one grid per process (astrea.py:155-190 loops over

@@ -90,46 +90,6 @@ __device__ __forceinline__ void recon_ppm(const A& at, const RH& rho, int r, T& 
   wR = R;
 }
 
-// The same limiter reading precomputed levels: ``F(x)`` is the face value at
-// x+1/2 and ``D(x)`` the second difference at x, each already evaluated at
-// every (boundary-mapped) index of the tile, so that d2c and d3 are not
-// recomputed for each of their several uses.  Same operations, same bits.
-template <typename T, class A, class AF, class AD, class RH>
-__device__ __forceinline__ void recon_ppm_levels(const A& at, const AF& F, const AD& D, const RH& rho, int r, T& wL,
-                                                 T& wR) {
-  const T C = T(1.25);
-  const int rm1 = rho(r - 1), rp1 = rho(r + 1), rm2 = rho(r - 2), rp2 = rho(r + 2);
-  const T w0 = at(r), wm1 = at(rm1), wp1 = at(rp1), wm2 = at(rm2), wp2 = at(rp2);
-  const T fL = F(rm1);
-  const T fR = F(r);
-  const T dwm = w0 - fL, dwp = fR - w0;
-  const T d2w = T(6) * ((fL - T(2) * w0) + fR);
-  const T d2c = D(r), d2c_m = D(rm1), d2c_p = D(rp1);
-  const T d3 = d2c_p - d2c;
-  const T d3_m1 = D(rho(rm1 + 1)) - d2c_m;
-  const T d3_m2 = D(rho(rm2 + 1)) - D(rm2);
-  const T d3_p2 = D(rho(rp2 + 1)) - D(rp2);
-  const bool extremum = (dwm * dwp <= T(0)) || ((w0 - wm2) * (wp2 - w0) <= T(0));
-  const T curv = npsign(d2c) * npmin(npmin(abs_(d2w), C * abs_(d2c)), npmin(C * abs_(d2c_p), C * abs_(d2c_m)));
-  const T d2w_lim = extremum ? curv : T(0);
-  const T scale = npmax(abs_(w0), npmax(npmax(abs_(wm1), abs_(wp1)), npmax(abs_(wm2), abs_(wp2))));
-  const bool sensitive = abs_(d2w) > T(1e-12) * scale;
-  const T phi = dvd(d2w_lim, d2w);
-  const T rl = sensitive ? phi : T(0);
-  const T d3min = npmin(npmin(d3_m1, d3), npmin(d3_m2, d3_p2));
-  const T d3max = npmax(npmax(d3_m1, d3), npmax(d3_m2, d3_p2));
-  const bool limit = (rl < T(1.0 - 1e-12)) || (T(.1) * npmax(abs_(d3max), abs_(d3min)) <= (d3max - d3min));
-  T L = fL, R = fR;
-  if ((dwm * dwp < T(0)) && limit) {
-    L = w0 - rl * dwm;
-    R = w0 + rl * dwp;
-  }
-  if (limit && abs_(dwm) >= T(2) * abs_(dwp)) L = (w0 - (T(2) * (T(1) - rl)) * dwp) - rl * dwm;
-  if (limit && abs_(dwp) >= T(2) * abs_(dwm)) R = (w0 + (T(2) * (T(1) - rl)) * dwm) + rl * dwp;
-  wL = L;
-  wR = R;
-}
-
 // WENO-JS, eps = 1e-6 (weno.py:22-149)
 template <typename T, class A, class RH>
 __device__ __forceinline__ void recon_weno3(const A& at, const RH& rho, int r, T& wL, T& wR) {

@@ -57,9 +57,6 @@ template <int SCH, int DIM, int TS, int TT> struct Geom {
   static constexpr int W_BEG = R_BEG - Reach<SCH>::L, W_END = R_END + Reach<SCH>::R;
   static constexpr int Q_BEG = W_BEG - (HO ? 1 : 0), Q_END = W_END + (HO ? 1 : 0);
   static constexpr int QW = TS + Q_END - Q_BEG, WW = TS + W_END - W_BEG, RW = TS + R_END - R_BEG;
-  // PPM levels: face values on [s0-2, s0+TS+2), second differences on [s0-3, s0+TS+5)
-  static constexpr int PF_BEG = R_BEG - 1, PF_W = TS + R_END - R_BEG + 1;
-  static constexpr int PD_BEG = R_BEG - 2, PD_W = TS + R_END - R_BEG + 5;
   static constexpr int YW = TS + 2;  // lambda of the interface averages right of cells s0-1 .. s0+TS
   static constexpr int KW = TS + 1;  // interfaces s0 .. s0+TS
   // transverse halos (2D): rows [t0-H, t0+TT+H)
@@ -78,9 +75,7 @@ template <int SCH, int DIM, int TS, int TT, int NV> struct Smem {
   static constexpr int n_F = NV * TT * G::KW;
   // the face arrays reuse the q level once it is dead; PCM reads raw q on faces, so it keeps q
   static constexpr int FA_OFF = SCH == PCM ? n_q : 0;
-  static constexpr int n_ppm = SCH == PPM ? NV * G::RH * (G::PF_W + G::PD_W) : 0;
-  static constexpr int n_r0a = (n_q + n_qw) > (FA_OFF + n_face + n_F) ? (n_q + n_qw) : (FA_OFF + n_face + n_F);
-  static constexpr int n_region0 = n_r0a > n_ppm ? n_r0a : n_ppm;
+  static constexpr int n_region0 = (n_q + n_qw) > (FA_OFF + n_face + n_F) ? (n_q + n_qw) : (FA_OFF + n_face + n_F);
   static constexpr int n_w = NV * G::WH * G::WW;
   static constexpr int n_R = 2 * NV * G::RH * G::RW;
   static constexpr int n_lam = G::FH * G::YW;
@@ -249,28 +244,6 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   }
   __syncthreads();
 
-  // ---- PPM: face values (ppm.py:38) and second differences (limiters.py:93) once per
-  // cell, into region 0 (the staged state is dead by now)
-  T* s_pf = sm;
-  T* s_pd = sm + NV * G::RH * G::PF_W;
-  if constexpr (SCH == PPM) {
-    constexpr int H = G::RH, WW = G::WW, WH = G::WH;
-    for (int e = tid; e < NV * H * (G::PF_W + G::PD_W); e += nth) {
-      const bool face = e < NV * H * G::PF_W;
-      const int e2 = face ? e : e - NV * H * G::PF_W;
-      const int W = face ? G::PF_W : G::PD_W;
-      const int s = e2 / (W * H), rem = e2 % (W * H);
-      const int row = rem / W, col = rem % W;
-      const int v = s0 + (face ? G::PF_BEG : G::PD_BEG) + col, vt = t0 - G::RT + row;
-      const int x = rs_(v), rt = DIM == 2 ? rt_(vt) : 0;
-      const T* wrow = s_w + (s * WH + (rt - (t0 - G::WT))) * WW - (s0 + G::W_BEG);
-      auto at = [&](int y) -> T { return wrow[y]; };
-      if (face) s_pf[(s * H + row) * G::PF_W + col] = ppm_face<T>(at, rs_, x);
-      else s_pd[(s * H + row) * G::PD_W + col] = ppm_d2c<T>(at, rs_, x);
-    }
-    __syncthreads();
-  }
-
   // ---- level R: reconstructed face values (wL at i-1/2, wR at i+1/2) of each cell
   {
     constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
@@ -282,23 +255,14 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       const T* wrow = s_w + (s * WH + (rt - (t0 - G::WT))) * WW - (s0 + G::W_BEG);
       auto at = [&](int x) -> T { return wrow[x]; };
       T wl, wr;
-      if constexpr (SCH == PPM) {
-        const int lr = rt - (t0 - G::RT);
-        const T* frow = s_pf + (s * H + lr) * G::PF_W - (s0 + G::PF_BEG);
-        const T* drow = s_pd + (s * H + lr) * G::PD_W - (s0 + G::PD_BEG);
-        auto F = [&](int x) -> T { return frow[x]; };
-        auto D = [&](int x) -> T { return drow[x]; };
-        recon_ppm_levels<T>(at, F, D, rs_, rs, wl, wr);
-      } else {
-        reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr);
-      }
+      reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr);
       s_R[((0 * NV + s) * H + row) * W + col] = wl;
       s_R[((1 * NV + s) * H + row) * W + col] = wr;
       if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) {
         // the face value the constrained transport uses: PPM's unlimited 4th-order
         // face (ppm.py:38-42), the right face value of the other schemes (weno.py:168, plm.py:39)
         T fv;
-        if constexpr (SCH == PPM) fv = s_pf[(s * H + (rt - (t0 - G::RT))) * G::PF_W + (rs - (s0 + G::PF_BEG))];
+        if constexpr (SCH == PPM) fv = ppm_face<T>(at, rs_, rs);
         else fv = wr;
         a.wface_out[M::var(s) * a.plane + gidx(vs, vt)] = fv;
       }

@@ -83,6 +83,19 @@ template <class M, typename T> __device__ __forceinline__ void p2c(const T* w, T
   q[5] = w[5]; q[6] = w[6]; q[7] = w[7];
 }
 
+// FP64 internal energy E - K of an FP32 conservative state.  Kept out of line so
+// that none of its FP64 work is hoisted into the common path of the callers.
+template <class M> __device__ __noinline__ float internal_energy_fp64(float q0, float q1, float q2, float q3, float q4,
+                                                                    float q5, float q6, float q7) {
+  const double rd = (double)q0;
+  const double vx = rd != 0.0 ? (double)q1 / rd : 0.0;
+  const double vy = M::VY ? (rd != 0.0 ? (double)q2 / rd : 0.0) : 0.0;
+  const double vz = M::VZ ? (rd != 0.0 ? (double)q3 / rd : 0.0) : 0.0;
+  double Kd = rd * ((vx * vx + vy * vy) + vz * vz);
+  if constexpr (M::MHD) Kd = Kd + (((double)q5 * q5 + (double)q6 * q6) + (double)q7 * q7);
+  return (float)((double)q4 - 0.5 * Kd);
+}
+
 // point_convert_conservative; in FP32 the internal energy of near-vacuum or
 // kinetic-dominated cells (E - K small against E) is recovered in FP64.
 template <class M, typename T> __device__ __forceinline__ void c2p(const T* q, T* w, T gm1) {
@@ -95,15 +108,8 @@ template <class M, typename T> __device__ __forceinline__ void c2p(const T* q, T
   T K = M::MHD ? T(.5) * (kin + nsq_mag<M>(q)) : T(.5) * kin;
   T e = q[4] - K;
   if constexpr (!Prec<T>::EXACT) {
-    if (!(e > T(1e-3) * abs_(q[4]))) {
-      double rd = (double)rho;
-      double vx = rd != 0.0 ? (double)q[1] / rd : 0.0;
-      double vy = M::VY ? (rd != 0.0 ? (double)q[2] / rd : 0.0) : 0.0;
-      double vz = M::VZ ? (rd != 0.0 ? (double)q[3] / rd : 0.0) : 0.0;
-      double Kd = rd * ((vx * vx + vy * vy) + vz * vz);
-      if constexpr (M::MHD) Kd = Kd + (((double)q[5] * q[5] + (double)q[6] * q[6]) + (double)q[7] * q[7]);
-      e = (T)((double)q[4] - 0.5 * Kd);
-    }
+    if (__builtin_expect(!(e > T(1e-3) * abs_(q[4])), 0))
+      e = internal_energy_fp64<M>(q[0], q[1], q[2], q[3], q[4], q[5], q[6], q[7]);
   }
   w[4] = gm1 * e;
   w[5] = q[5]; w[6] = q[6]; w[7] = q[7];

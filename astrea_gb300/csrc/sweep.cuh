@@ -113,9 +113,11 @@ template <typename T> __device__ __forceinline__ T combine(int integ, int stage,
   }
 }
 
+// Block maximum in T (converting a float to double is exact and monotone, so the
+// maximum of the floats is the maximum of their doubles), one atomic per CTA.
 template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, unsigned long long* dst) {
-  __shared__ double red[32];
-  double x = (double)v;
+  __shared__ T red[32];
+  T x = v;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x = npmax(x, __shfl_xor_sync(0xffffffffu, x, o));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -123,10 +125,10 @@ template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, un
   __syncthreads();
   if (wid == 0) {
     const int nw = (blockDim.x + 31) >> 5;
-    double y = lane < nw ? red[lane] : 0.0;
+    T y = lane < nw ? red[lane] : T(0);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) y = npmax(y, __shfl_xor_sync(0xffffffffu, y, o));
-    if (lane == 0) atomicMax(dst, (unsigned long long)__double_as_longlong(y));
+    if (lane == 0) atomicMax(dst, (unsigned long long)__double_as_longlong((double)y));
   }
 }
 

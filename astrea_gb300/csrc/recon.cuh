@@ -54,21 +54,15 @@ template <typename T, class A, class RH> __device__ __forceinline__ T ppm_d3(con
 // For finite data the limiter's no-extremum-anywhere branch
 // (limiters.py:141-143) gives the same values as the main branch, so the main
 // branch is evaluated for every cell.
-template <typename T, class A, class RH>
-__device__ __forceinline__ void recon_ppm(const A& at, const RH& rho, int r, T& wL, T& wR) {
+// The McCorquodale & Colella limiter of one cell from its stencil values:
+// w at r-2..r+2, the unlimited faces at r-1/2 and r+1/2, second differences
+// d2c at r-1..r+1 and third differences d3 at r-2, r-1, r, r+2.
+template <typename T>
+__device__ __forceinline__ void ppm_mc_limit(T w0, T wm1, T wp1, T wm2, T wp2, T fL, T fR, T d2c_m, T d2c, T d2c_p,
+                                             T d3_m2, T d3_m1, T d3, T d3_p2, T& wL, T& wR) {
   const T C = T(1.25);
-  const T w0 = at(r), wm1 = at(rho(r - 1)), wp1 = at(rho(r + 1)), wm2 = at(rho(r - 2)), wp2 = at(rho(r + 2));
-  const T fL = ppm_face<T>(at, rho, rho(r - 1));
-  const T fR = ppm_face<T>(at, rho, r);
   const T dwm = w0 - fL, dwp = fR - w0;
   const T d2w = T(6) * ((fL - T(2) * w0) + fR);
-  const T d2c = (wm1 - T(2) * w0) + wp1;
-  const T d2c_m = ppm_d2c<T>(at, rho, rho(r - 1));
-  const T d2c_p = ppm_d2c<T>(at, rho, rho(r + 1));
-  const T d3 = ppm_d3<T>(at, rho, r);
-  const T d3_m1 = ppm_d3<T>(at, rho, rho(r - 1));
-  const T d3_m2 = ppm_d3<T>(at, rho, rho(r - 2));
-  const T d3_p2 = ppm_d3<T>(at, rho, rho(r + 2));
   const bool extremum = (dwm * dwp <= T(0)) || ((w0 - wm2) * (wp2 - w0) <= T(0));
   const T curv = npsign(d2c) * npmin(npmin(abs_(d2w), C * abs_(d2c)), npmin(C * abs_(d2c_p), C * abs_(d2c_m)));
   const T d2w_lim = extremum ? curv : T(0);
@@ -88,6 +82,55 @@ __device__ __forceinline__ void recon_ppm(const A& at, const RH& rho, int r, T& 
   if (limit && abs_(dwp) >= T(2) * abs_(dwm)) R = (w0 + (T(2) * (T(1) - rl)) * dwm) + rl * dwp;
   wL = L;
   wR = R;
+}
+
+// PPM faces with the McCorquodale & Colella extremum-preserving limiter
+// (ppm.py:30-72 with author 'mc'; limiters.extrapolant_limiter, limiters.py:82-143).
+// For finite data the limiter's no-extremum-anywhere branch
+// (limiters.py:141-143) gives the same values as the main branch, so the main
+// branch is evaluated for every cell.
+template <typename T, class A, class RH>
+__device__ __forceinline__ void recon_ppm(const A& at, const RH& rho, int r, T& wL, T& wR) {
+  const T w0 = at(r), wm1 = at(rho(r - 1)), wp1 = at(rho(r + 1)), wm2 = at(rho(r - 2)), wp2 = at(rho(r + 2));
+  const T fL = ppm_face<T>(at, rho, rho(r - 1));
+  const T fR = ppm_face<T>(at, rho, r);
+  const T d2c = (wm1 - T(2) * w0) + wp1;
+  const T d2c_m = ppm_d2c<T>(at, rho, rho(r - 1));
+  const T d2c_p = ppm_d2c<T>(at, rho, rho(r + 1));
+  const T d3 = ppm_d3<T>(at, rho, r);
+  const T d3_m1 = ppm_d3<T>(at, rho, rho(r - 1));
+  const T d3_m2 = ppm_d3<T>(at, rho, rho(r - 2));
+  const T d3_p2 = ppm_d3<T>(at, rho, rho(r + 2));
+  ppm_mc_limit<T>(w0, wm1, wp1, wm2, wp2, fL, fR, d2c_m, d2c, d2c_p, d3_m2, d3_m1, d3, d3_p2, wL, wR);
+}
+
+// The same reconstruction for K consecutive cells r0 .. r0+K-1 where no index
+// needs a boundary map (interior or periodic tiles): the cells' stencils
+// overlap, so every face value, second and third difference is computed once
+// and shared instead of once per cell that uses it.  Same expressions, same
+// results.  ``out(k, wL, wR, fR)`` receives cell r0+k and its unlimited face
+// value at r0+k+1/2.
+template <typename T, int K, class A, class OUT>
+__device__ __forceinline__ void recon_ppm_strip(const A& at, int r0, const OUT& out) {
+  T w[K + 7];     // x = r0-3 .. r0+K+3
+  T d2[K + 5];    // x = r0-2 .. r0+K+2
+  T d3[K + 4];    // x = r0-2 .. r0+K+1
+  T f[K + 1];     // faces at x+1/2, x = r0-1 .. r0+K-1
+#pragma unroll
+  for (int i = 0; i < K + 7; ++i) w[i] = at(r0 - 3 + i);
+#pragma unroll
+  for (int j = 0; j < K + 5; ++j) d2[j] = (w[j] - T(2) * w[j + 1]) + w[j + 2];
+#pragma unroll
+  for (int j = 0; j < K + 4; ++j) d3[j] = d2[j + 1] - d2[j];
+#pragma unroll
+  for (int j = 0; j < K + 1; ++j) f[j] = T(7.0 / 12.0) * (w[j + 2] + w[j + 3]) - T(1.0 / 12.0) * (w[j + 1] + w[j + 4]);
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    T wl, wr;
+    ppm_mc_limit<T>(w[k + 3], w[k + 2], w[k + 4], w[k + 1], w[k + 5], f[k], f[k + 1], d2[k + 1], d2[k + 2],
+                    d2[k + 3], d3[k], d3[k + 1], d3[k + 2], d3[k + 4], wl, wr);
+    out(k, wl, wr, f[k + 1]);
+  }
 }
 
 // WENO-JS, eps = 1e-6 (weno.py:22-149)

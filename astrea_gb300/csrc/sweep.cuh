@@ -49,6 +49,13 @@ template <typename T> struct SweepArgs {
   T* wface_out;       // optional (2D MHD): face value at i+1/2 of every cell, physical layout [8][n0][n1]
 };
 
+// Cells per thread in the shared-stencil PPM level of a 2D tile: a divisor of the
+// level width (7 or 5), or 1 (per-cell evaluation).  1D tiles keep one cell per
+// thread: they have too few rows to fill a CTA with strips.
+template <int RW, int DIM> struct PpmStrip {
+  static constexpr int K = DIM != 2 ? 1 : (RW % 7 == 0 ? 7 : (RW % 5 == 0 ? 5 : 1));
+};
+
 template <int SCH, int DIM, int TS, int TT> struct Geom {
   static constexpr bool HO = SCH >= PPM;  // 4th-order conversions (generic.py:250-255)
   static constexpr bool ROE = SCH >= PPM; // Roe-type interface average for the wave speed
@@ -247,7 +254,26 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   __syncthreads();
 
   // ---- level R: reconstructed face values (wL at i-1/2, wR at i+1/2) of each cell
-  {
+  if constexpr (SCH == PPM && !CL && PpmStrip<G::RW, DIM>::K > 1) {
+    // no boundary map on this tile: one thread per strip of K cells shares the stencil work
+    constexpr int K = PpmStrip<G::RW, DIM>::K, NS = G::RW / K;
+    constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
+    for (int e = tid; e < NS * H * NV; e += nth) {
+      const int s = e / (NS * H), rem = e % (NS * H);
+      const int row = rem / NS, col0 = (rem % NS) * K;
+      const int vs0 = s0 + G::R_BEG + col0, vt = t0 - G::RT + row;
+      const T* wrow = s_w + (s * WH + row + (G::WT - G::RT)) * WW - (s0 + G::W_BEG);
+      T* rl = s_R + ((0 * NV + s) * H + row) * W + col0;
+      T* rr = s_R + ((1 * NV + s) * H + row) * W + col0;
+      recon_ppm_strip<T, K>([&](int x) -> T { return wrow[x]; }, vs0, [&](int k, T wl, T wr, T fr) {
+        rl[k] = wl;
+        rr[k] = wr;
+        const int vs = vs0 + k;
+        if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt)
+          a.wface_out[M::var(s) * a.plane + gidx(vs, vt)] = fr;
+      });
+    }
+  } else {
     constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
     for (int e = tid; e < W * H * NV; e += nth) {
       const int s = e / (W * H), rem = e % (W * H);

@@ -307,11 +307,16 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   };
 
   // ---- level lambda: wave speed of the interface average right of each cell (fv.compute_eigen)
-  {
-    constexpr int W = G::YW, H = G::FH;
+  // LLF reads the speeds on both sides of every interface of the face levels; the
+  // HLL-type solvers use them only for the tile maximum (the time step), so they
+  // evaluate the tile's own cells, and only when that maximum is wanted.
+  constexpr bool LAM_ALL = SOL == LLF;
+  if (LAM_ALL || a.want_emax) {
+    constexpr int W = LAM_ALL ? G::YW : TS, H = LAM_ALL ? G::FH : TT;
+    constexpr int C_OFF = LAM_ALL ? 0 : 1, R_OFF = LAM_ALL ? 0 : G::FT;
     T lmax = T(0);
     for (int e = tid; e < W * H; e += nth) {
-      const int row = e / W, col = e % W;
+      const int row = e / W + R_OFF, col = e % W + C_OFF;
       const int vj = s0 - 1 + col, vt = t0 - G::FT + row;
       const int rj = rs_(vj), rt = DIM == 2 ? rt_(vt) : 0;
       T y[8];
@@ -325,7 +330,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         else arith_avg<M>(wp, wm, y);
       }
       const T lam = max_speed<M, DIM == 1 ? 0 : AX>(y, gamma);
-      s_lam[row * W + col] = lam;
+      if constexpr (LAM_ALL) s_lam[row * G::YW + col] = lam;
       if (a.want_emax && vj >= s0 && vj < s0 + TS && vj < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) lmax = npmax(lmax, lam);
     }
     if (a.want_emax) block_max_to_clock(lmax, &a.clock->emax[DIM == 1 ? 0 : AX]);

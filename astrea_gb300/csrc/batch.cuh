@@ -50,7 +50,7 @@ template <int MID, int DIM, int TS, int TT, typename T> constexpr size_t batch_s
 }
 
 template <typename T, int MID, int DIM, int AX, int TS, int TT>
-__global__ void __launch_bounds__(256, SweepOcc<T, MID>::value) batched_sweep_kernel(const BatchArgs<T> b) {
+__global__ void __launch_bounds__(256, (SweepOcc<T, MID, 256>::value)) batched_sweep_kernel(const BatchArgs<T> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   constexpr int HLL = MID == 8 ? HLLD : HLLC;

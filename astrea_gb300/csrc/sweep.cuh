@@ -142,7 +142,7 @@ template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, un
 // One tile: cells [s0, s0+TS) along the sweep and rows [t0, t0+TT) across it.
 // Called by the single-grid kernel (one tile per CTA) and by the batched
 // persistent kernel (a work list of tiles of many grids).
-template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, bool CL>
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, bool CL, int NT>
 __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int s0, const int t0,
                                                 unsigned char* __restrict__ smem_raw) {
   using M = Model<MID>;
@@ -167,7 +167,9 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     rt_ = make_rho(a.bc, Nt);
   }
   const T gamma = a.gamma, gm1 = a.gm1;
-  const int tid = threadIdx.x, nth = blockDim.x;
+  // the CTA size is a compile-time constant, so the per-level loops have known trip counts
+  const int tid = threadIdx.x;
+  constexpr int nth = NT;
   // axis label of this sweep: its position in the step's iteration order
   const int label = a.physical ? (DIM == 1 ? 0 : AX)
                   : (a.label >= 0 ? a.label : (DIM == 1 ? 0 : (AX == 0 ? a.clock->order : 1 - a.clock->order)));
@@ -512,7 +514,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 
 // Clamping is only needed on outflow grids, for tiles whose widest level
 // (the staged state) reaches past the grid edge.
-template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT>
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT = (DIM == 1 ? 64 : 256)>
 __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, const int t0,
                                            unsigned char* __restrict__ smem_raw) {
   using G = Geom<SCH, DIM, TS, TT>;
@@ -520,18 +522,20 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
   const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
   const bool inside = s0 + G::Q_BEG >= 0 && s0 + TS + G::Q_END <= Ns &&
                       (DIM == 1 || (t0 - G::QT >= 0 && t0 + TT + G::QT <= Nt));
-  if (a.bc == EDGE && !inside) sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, true>(a, s0, t0, smem_raw);
-  else sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false>(a, s0, t0, smem_raw);
+  if (a.bc == EDGE && !inside) sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, true, NT>(a, s0, t0, smem_raw);
+  else sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT>(a, s0, t0, smem_raw);
 }
 
-// FP32 Euler tiles fit four CTAs per SM (<= 64 registers); FP64 and MHD tiles are larger
-template <typename T, int MID> struct SweepOcc { static constexpr int value = (sizeof(T) == 4 && MID != 8) ? 4 : 1; };
+// FP32 Euler tiles fit 1024 threads per SM (<= 64 registers); FP64 and MHD tiles are larger
+template <typename T, int MID, int NT> struct SweepOcc {
+  static constexpr int value = (sizeof(T) == 4 && MID != 8) ? (1024 / NT > 0 ? 1024 / NT : 1) : 1;
+};
 
-template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT>
-__global__ void __launch_bounds__(256, SweepOcc<T, MID>::value) sweep_kernel(const SweepArgs<T> a) {
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT>
+__global__ void __launch_bounds__(NT, (SweepOcc<T, MID, NT>::value)) sweep_kernel(const SweepArgs<T> a) {
   if (a.clock->done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT>(a, blockIdx.x * TS, blockIdx.y * TT, smem_raw);
+  sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT, NT>(a, blockIdx.x * TS, blockIdx.y * TT, smem_raw);
 }
 
 }  // namespace astrea

@@ -22,7 +22,7 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
   constexpr int TS = DIM == 1 ? TS1 : TS2, TT = DIM == 1 ? 1 : TT2, NT = DIM == 1 ? NT1 : NT2;
   constexpr size_t bytes = sweep_smem_bytes<T, MID, SCH, DIM>();
   static_assert(bytes <= 227 * 1024, "sweep tile exceeds the shared memory of one CTA");
-  auto k = sweep_kernel<T, MID, SCH, SOL, DIM, AX, TS, TT>;
+  auto k = sweep_kernel<T, MID, SCH, SOL, DIM, AX, TS, TT, NT>;
   int dev = 0;
   cudaGetDevice(&dev);
   static unsigned long long configured = 0ull;  // one bit per device

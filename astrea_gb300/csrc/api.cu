@@ -168,6 +168,10 @@ template <typename T> struct Engine final : IEngine {
     a.dx = cfg.dx;
     a.clock = c;
     a.physical = (cfg.flags & ASTREA_FLAG_PHYSICAL) ? 1 : 0;
+    a.flatten = (cfg.flags & ASTREA_FLAG_FLATTEN) ? 1 : 0;
+    a.viscosity = (cfg.flags & ASTREA_FLAG_VISCOSITY) ? 1 : 0;
+    a.av_alpha = T(0.3);
+    a.av_beta = T(0.3);
     return a;
   }
 
@@ -380,6 +384,8 @@ static int validate(const astrea_cfg* c) {
   if (c->boundary != EDGE && c->boundary != WRAP) return fail(ASTREA_ERR_CONFIG, "boundary must be edge(0) or wrap(1)");
   if ((c->flags & ASTREA_FLAG_CT) && (c->dim != 2 || c->model != 8))
     return fail(ASTREA_ERR_CONFIG, "constrained transport needs dim 2 and model 8");
+  if ((c->flags & ASTREA_FLAG_CT) && (c->flags & ASTREA_FLAG_FLATTEN) && c->scheme == PPM)
+    return fail(ASTREA_ERR_CONFIG, "PPM flattening is not available with constrained transport");
   if (!(c->dx > 0) || !(c->cfl > 0) || !(c->gamma > 1) || c->checkpoints < 1)
     return fail(ASTREA_ERR_CONFIG, "dx, cfl > 0, gamma > 1, checkpoints >= 1 required");
   if ((long long)c->n0 * (long long)(c->dim == 2 ? c->n1 : 1) > (1LL << 31))

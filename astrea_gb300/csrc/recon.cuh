@@ -15,7 +15,9 @@ namespace astrea {
 template <int SCH> struct Reach;
 template <> struct Reach<PCM> { static constexpr int L = 0, R = 0; };
 template <> struct Reach<PLM> { static constexpr int L = 1, R = 1; };
-template <> struct Reach<PPM> { static constexpr int L = 3, R = 4; };
+// PPM: the faces need 2 cells each side and the limiter 2 more; optional flattening
+// reads pressure 3 cells beyond the face range, hence one more on the left.
+template <> struct Reach<PPM> { static constexpr int L = 4, R = 4; };
 template <> struct Reach<WENO3> { static constexpr int L = 1, R = 1; };
 template <> struct Reach<WENO5> { static constexpr int L = 2, R = 2; };
 template <> struct Reach<WENO7> { static constexpr int L = 3, R = 3; };
@@ -89,11 +91,20 @@ __device__ __forceinline__ void ppm_mc_limit(T w0, T wm1, T wp1, T wm2, T wp2, T
 // For finite data the limiter's no-extremum-anywhere branch
 // (limiters.py:141-143) gives the same values as the main branch, so the main
 // branch is evaluated for every cell.
+// A face value at x+1/2 blended towards the cell value at x by the flattening
+// coefficient eta(x) (ppm.py:67 with apply_flattener): f * eta + w * (1 - eta).
+template <typename T> __device__ __forceinline__ T ppm_flatten(T f, T w, T eta) { return f * eta + w * (T(1) - eta); }
+
+// ``eta`` (nullptr: no flattening) gives the flattening coefficient at a mapped cell index.
 template <typename T, class A, class RH>
-__device__ __forceinline__ void recon_ppm(const A& at, const RH& rho, int r, T& wL, T& wR) {
+__device__ __forceinline__ void recon_ppm(const A& at, const RH& rho, int r, T& wL, T& wR, const T* eta = nullptr) {
   const T w0 = at(r), wm1 = at(rho(r - 1)), wp1 = at(rho(r + 1)), wm2 = at(rho(r - 2)), wp2 = at(rho(r + 2));
-  const T fL = ppm_face<T>(at, rho, rho(r - 1));
-  const T fR = ppm_face<T>(at, rho, r);
+  T fL = ppm_face<T>(at, rho, rho(r - 1));
+  T fR = ppm_face<T>(at, rho, r);
+  if (eta) {
+    fL = ppm_flatten<T>(fL, wm1, eta[rho(r - 1)]);
+    fR = ppm_flatten<T>(fR, w0, eta[r]);
+  }
   const T d2c = (wm1 - T(2) * w0) + wp1;
   const T d2c_m = ppm_d2c<T>(at, rho, rho(r - 1));
   const T d2c_p = ppm_d2c<T>(at, rho, rho(r + 1));
@@ -111,7 +122,7 @@ __device__ __forceinline__ void recon_ppm(const A& at, const RH& rho, int r, T& 
 // results.  ``out(k, wL, wR, fR)`` receives cell r0+k and its unlimited face
 // value at r0+k+1/2.
 template <typename T, int K, class A, class OUT>
-__device__ __forceinline__ void recon_ppm_strip(const A& at, int r0, const OUT& out) {
+__device__ __forceinline__ void recon_ppm_strip(const A& at, int r0, const OUT& out, const T* eta = nullptr) {
   T w[K + 7];     // x = r0-3 .. r0+K+3
   T d2[K + 5];    // x = r0-2 .. r0+K+2
   T d3[K + 4];    // x = r0-2 .. r0+K+1
@@ -124,6 +135,10 @@ __device__ __forceinline__ void recon_ppm_strip(const A& at, int r0, const OUT& 
   for (int j = 0; j < K + 4; ++j) d3[j] = d2[j + 1] - d2[j];
 #pragma unroll
   for (int j = 0; j < K + 1; ++j) f[j] = T(7.0 / 12.0) * (w[j + 2] + w[j + 3]) - T(1.0 / 12.0) * (w[j + 1] + w[j + 4]);
+  if (eta) {
+#pragma unroll
+    for (int j = 0; j < K + 1; ++j) f[j] = ppm_flatten<T>(f[j], w[j + 2], eta[r0 - 1 + j]);
+  }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     T wl, wr;
@@ -217,10 +232,11 @@ __device__ __forceinline__ void recon_weno7(const A& at, const RH& rho, int r, T
 }
 
 template <int SCH, typename T, class A, class RH>
-__device__ __forceinline__ void reconstruct(const A& at, const RH& rho, int r, int limiter, T& wL, T& wR) {
+__device__ __forceinline__ void reconstruct(const A& at, const RH& rho, int r, int limiter, T& wL, T& wR,
+                                            const T* eta = nullptr) {
   if constexpr (SCH == PCM) { wL = wR = at(r); }
   else if constexpr (SCH == PLM) recon_plm<T>(at, rho, r, limiter, wL, wR);
-  else if constexpr (SCH == PPM) recon_ppm<T>(at, rho, r, wL, wR);
+  else if constexpr (SCH == PPM) recon_ppm<T>(at, rho, r, wL, wR, eta);
   else if constexpr (SCH == WENO3) recon_weno3<T>(at, rho, r, wL, wR);
   else if constexpr (SCH == WENO5) recon_weno5<T>(at, rho, r, wL, wR);
   else recon_weno7<T>(at, rho, r, wL, wR);

@@ -47,7 +47,17 @@ template <typename T> struct SweepArgs {
   Clock* clock;
   T* flux_out;        // optional: interface fluxes [NV][Ns+1][Nt]
   T* wface_out;       // optional (2D MHD): face value at i+1/2 of every cell, physical layout [8][n0][n1]
+  int flatten;        // PPM: Colella (1990) flattening of the face values
+  int viscosity;      // PPM: McCorquodale & Colella (2011) artificial viscosity added to the fluxes
+  T av_alpha, av_beta;
 };
+
+// plane index of primitive variable v in model M (-1 if M does not store it)
+template <class M> __host__ __device__ constexpr int plane_of(int v) {
+  for (int s = 0; s < M::NV; ++s)
+    if (M::var(s) == v) return s;
+  return -1;
+}
 
 // Cells per thread in the shared-stencil PPM level of a 2D tile: a divisor of the
 // level width (7 or 5), or 1 (per-cell evaluation).  1D tiles keep one cell per
@@ -86,7 +96,19 @@ template <int SCH, int DIM, int TS, int TT, int NV> struct Smem {
   static constexpr int n_w = NV * G::WH * G::WW;
   static constexpr int n_R = 2 * NV * G::RH * G::RW;
   static constexpr int n_lam = G::FH * G::YW;
-  static constexpr int total = n_region0 + n_w + n_R + n_lam + 64;
+  static constexpr int base = n_region0 + n_w + n_R + n_lam + 64;
+  // PPM extras: flattening coefficients on the rows of the face level and the
+  // columns [s0-2, s0+TS+2), and the viscous face fluxes of the tile's interfaces.
+  // In 2D the viscous fluxes sit where the final fluxes go (they are added there),
+  // and the coefficients in the gap of region 0 between the staged state and the
+  // face arrays; otherwise both go past the end.
+  static constexpr int n_eta = SCH == PPM ? G::RH * (G::RW + 1) : 0;
+  static constexpr int n_mu = SCH == PPM ? NV * TT * G::KW : 0;
+  static constexpr bool MU_IN_F = DIM == 2;
+  static constexpr bool ETA_IN_GAP = DIM == 2 && (n_q + n_qw + n_eta <= FA_OFF + n_face);
+  static constexpr int MU_OFF = MU_IN_F ? FA_OFF + n_face : base;
+  static constexpr int ETA_OFF = ETA_IN_GAP ? n_q + n_qw : base + (MU_IN_F ? 0 : n_mu);
+  static constexpr int total = base + (MU_IN_F ? 0 : n_mu) + (ETA_IN_GAP ? 0 : n_eta);
 };
 
 template <class M, typename T> __device__ __forceinline__ void load_sm(const T* base, int stride, int idx, T* x) {
@@ -255,6 +277,84 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   }
   __syncthreads();
 
+  // ---- PPM extras (optional): flattening coefficients (ppm.apply_flattener,
+  // ppm.py:111-134) and artificial-viscosity face fluxes (ppm.apply_artificial_viscosity,
+  // ppm.py:138-170).  Neither runs in the reference (its code for them fails); the
+  // kernels follow those formulas with the two corrections from the cited papers
+  // that the oracle makes (strong compressive jumps only; no second factor dx).
+  T* s_eta = sm + S::ETA_OFF;
+  T* s_mu = sm + S::MU_OFF;
+  if constexpr (SCH == PPM) {
+    if (a.flatten || a.viscosity) {
+      constexpr int PP = plane_of<M>(4), PR = plane_of<M>(0);
+      constexpr int PN = plane_of<M>(1 + (DIM == 1 ? 0 : AX));
+      constexpr int PT = DIM == 2 ? plane_of<M>(1 + (1 - AX)) : 0;
+      // w level at real column x and real row rt
+      auto wv = [&](int pl, int x, int rt) -> T {
+        return s_w[(pl * G::WH + (rt - (t0 - G::WT))) * G::WW + (x - (s0 + G::W_BEG))];
+      };
+      if (a.flatten) {
+        constexpr int W = G::RW + 1, H = G::RH;
+        constexpr double DZ = 0.85 - 0.75;
+        for (int e = tid; e < W * H; e += nth) {
+          const int row = e / W, col = e % W;
+          const int vx = s0 + G::R_BEG - 1 + col, vt = t0 - G::RT + row;
+          const int x = rs_(vx), rt = DIM == 2 ? rt_(vt) : 0;
+          auto P = [&](int y) -> T { return wv(PP, y, rt); };
+          // chi_bar at real cell y (every difference padded on its own)
+          auto chi_bar = [&](int y) -> T {
+            const T dp1 = P(rs_(y + 1)) - P(rs_(y - 1));
+            const T dp2 = P(rs_(y + 2)) - P(rs_(y - 2));
+            const T z = dvd(abs_(dp1), abs_(dp2));
+            T cb = T(1) - dvd(z - T(.75), T(DZ));
+            if (z > T(.85)) cb = T(0);
+            if (z < T(.75)) cb = T(1);
+            // only strong, compressive pressure jumps are flattened (Colella & Woodward 1984, A.1)
+            const bool not_compressive = (wv(PN, rs_(y - 1), rt) - wv(PN, rs_(y + 1), rt)) <= T(0);
+            const bool weak = dvd(abs_(dp1), npmin(P(rs_(y + 1)), P(rs_(y - 1)))) <= T(.33);
+            if (not_compressive || weak) cb = T(1);
+            return cb;
+          };
+          const T cb = chi_bar(x);
+          const T sgn = npsign(P(rs_(x + 1)) - P(rs_(x - 1)));
+          T chi = cb;
+          if (sgn < T(0)) chi = npmin(cb, chi_bar(rs_(x + 1)));
+          if (sgn > T(0)) chi = npmin(cb, chi_bar(rs_(x - 1)));
+          s_eta[row * W + col] = chi;
+        }
+      }
+      if (a.viscosity) {
+        // mu at face x+1/2 for the interface right of cell x = rho(vk-1)
+        constexpr int W = G::KW;
+        for (int e = tid; e < W * TT; e += nth) {
+          const int row = e / W, col = e % W;
+          const int vk = s0 + col, vt = t0 + row;
+          const int rt = DIM == 2 ? rt_(vt) : 0;
+          const int x = rs_(vk - 1), xp = rs_(x + 1);
+          T lam = wv(PN, xp, rt) - wv(PN, x, rt);
+          if constexpr (DIM == 2) {
+            const int rm = rt_(rt - 1), rp = rt_(rt + 1);
+            const T dvt_x = wv(PT, x, rp) - wv(PT, x, rm);
+            const T dvt_xp = wv(PT, xp, rp) - wv(PT, xp, rm);
+            lam = lam + T(.25) * (dvt_xp + dvt_x);
+          }
+          const T cs_x = sqrt_(dvd(gamma * wv(PP, x, rt), wv(PR, x, rt)));
+          const T cs_xp = sqrt_(dvd(gamma * wv(PP, xp, rt), wv(PR, xp, rt)));
+          const T cmin = npmin(cs_x, cs_xp);
+          T nu = npmin(T(1), dvd(lam * lam, a.av_beta * (cmin * cmin))) * lam;
+          if (lam >= T(0)) nu = T(0);
+          const T* qrow = s_q + (rt - (t0 - G::QT)) * G::QW - (s0 + G::Q_BEG);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            const T* qv = qrow + v * G::QH * G::QW;
+            s_mu[(v * TT + row) * W + col] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+
   // ---- level R: reconstructed face values (wL at i-1/2, wR at i+1/2) of each cell
   if constexpr (SCH == PPM && !CL && PpmStrip<G::RW, DIM>::K > 1) {
     // no boundary map on this tile: one thread per strip of K cells shares the stencil work
@@ -267,13 +367,14 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       const T* wrow = s_w + (s * WH + row + (G::WT - G::RT)) * WW - (s0 + G::W_BEG);
       T* rl = s_R + ((0 * NV + s) * H + row) * W + col0;
       T* rr = s_R + ((1 * NV + s) * H + row) * W + col0;
+      const T* erow = a.flatten ? s_eta + row * (W + 1) - (s0 + G::R_BEG - 1) : nullptr;
       recon_ppm_strip<T, K>([&](int x) -> T { return wrow[x]; }, vs0, [&](int k, T wl, T wr, T fr) {
         rl[k] = wl;
         rr[k] = wr;
         const int vs = vs0 + k;
         if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt)
           a.wface_out[M::var(s) * a.plane + gidx(vs, vt)] = fr;
-      });
+      }, erow);
     }
   } else {
     constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
@@ -284,15 +385,17 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       const int rs = rs_(vs), rt = DIM == 2 ? rt_(vt) : 0;
       const T* wrow = s_w + (s * WH + (rt - (t0 - G::WT))) * WW - (s0 + G::W_BEG);
       auto at = [&](int x) -> T { return wrow[x]; };
+      const T* erow = (SCH == PPM && a.flatten) ? s_eta + row * (W + 1) - (s0 + G::R_BEG - 1) : nullptr;
       T wl, wr;
-      reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr);
+      reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr, erow);
       s_R[((0 * NV + s) * H + row) * W + col] = wl;
       s_R[((1 * NV + s) * H + row) * W + col] = wr;
       if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) {
         // the face value the constrained transport uses: PPM's unlimited 4th-order
         // face (ppm.py:38-42), the right face value of the other schemes (weno.py:168, plm.py:39)
         T fv;
-        if constexpr (SCH == PPM) fv = ppm_face<T>(at, rs_, rs);
+        if constexpr (SCH == PPM) fv = erow ? ppm_flatten<T>(ppm_face<T>(at, rs_, rs), at(rs), erow[rs])
+                                          : ppm_face<T>(at, rs_, rs);
         else fv = wr;
         a.wface_out[M::var(s) * a.plane + gidx(vs, vt)] = fv;
       }
@@ -402,6 +505,12 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       make_flux<M, 0>(wm, fm, gamma, gm1);
       if constexpr (SOL == HLLD) load_wS(rs_(vk), 0, wSr);
       solve(e, 0, wSr, wp, wm, qp, qm, fp, fm, F);
+      if constexpr (SCH == PPM) {
+        if (a.viscosity) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + s_mu[v * TT * W + e];
+        }
+      }
       store_sm<M>(s_F, TT * W, e, F);
     }
   } else {
@@ -464,6 +573,13 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       T F[8];
 #pragma unroll
       for (int i = 0; i < 8; ++i) F[i] = Fc[i] - T(C24) * ((xp[i] - x0[i]) - (x0[i] - xm[i]));
+      if constexpr (SCH == PPM) {
+        // the viscous flux of this interface sits where F goes: read it, then overwrite
+        if (a.viscosity) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + s_mu[(v * TT + row) * W + col];
+        }
+      }
       store_sm<M>(s_F, TT * W, row * W + col, F);
     }
   }

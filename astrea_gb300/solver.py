@@ -41,6 +41,8 @@ class RunConfig:
     checkpoints: int = 1
     compat: bool = True  # False: textbook HLLC/HLLD (not a reference option)
     magnetic_2d: bool = False  # constrained-transport 2D MHD (sim_variables.magnetic_2d)
+    flatten: bool = False  # PPM flattening (schemes/ppm.py:111-134; not run by the reference)
+    viscosity: bool = False  # PPM artificial viscosity (schemes/ppm.py:138-170; not run by the reference)
 
     def to_c(self):
         if self.solver not in C.SOLVER or self.solver == "lw":
@@ -52,7 +54,8 @@ class RunConfig:
                         integrator=C.INTEGRATOR[self.integrator], boundary=C.BOUNDARY[self.boundary],
                         limiter=C.LIMITER[self.limiter], gamma=float(self.gamma), dx=float(self.dx),
                         cfl=float(self.cfl), t_end=float(self.t_end), checkpoints=int(self.checkpoints),
-                        flags=(0 if self.compat else 1) | (2 if self.magnetic_2d else 0))
+                        flags=(0 if self.compat else 1) | (2 if self.magnetic_2d else 0)
+                        | (4 if self.flatten else 0) | (8 if self.viscosity else 0))
 
     @property
     def shape(self):

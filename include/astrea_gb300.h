@@ -76,6 +76,18 @@ typedef struct astrea_cfg {
  * transport (sim_variables.magnetic_2d; num_methods/mag_field.py).  Requires
  * dim 2 and model 8. */
 #define ASTREA_FLAG_CT 2
+/* ASTREA_FLAG_FLATTEN / ASTREA_FLAG_VISCOSITY (PPM only; other schemes ignore
+ * them): Colella (1990) flattening of the face values and McCorquodale &
+ * Colella (2011) artificial viscosity (alpha = beta = 0.3) added to the
+ * fluxes, after schemes/ppm.py:111-170 (apply_flattener,
+ * apply_artificial_viscosity).  The reference never runs that code (it fails
+ * when called).  These follow its formulas with two corrections from the
+ * papers it cites: flattening acts only on strong, compressive pressure jumps
+ * (Colella & Woodward 1984, A.1), and the viscosity coefficient uses the face
+ * velocity difference without a second factor dx.  Flattening is not
+ * available with constrained transport. */
+#define ASTREA_FLAG_FLATTEN 4
+#define ASTREA_FLAG_VISCOSITY 8
 
 typedef struct astrea_handle astrea_handle;
 

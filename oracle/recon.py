@@ -48,11 +48,19 @@ def ppm_face(wS, bc):
 
 
 def flatten_coefficient(wS, axis, bc, delta=.33, z0=.75, z1=.85):
-    """Colella (1990) flattening coefficient chi per cell.
+    """Flattening coefficient chi per cell (1: keep the PPM faces, 0: flat).
 
     The reference's ``apply_flattener`` (ppm.py:111-134) cannot run (it
-    returns an (N,8) array that the caller broadcasts against (N,8) again);
-    this follows its formulas with chi kept per cell.  Parity unpinned.
+    returns an (N,8) array that the caller broadcasts against (N,8) again).
+    This follows its formulas -- chi_bar = 1 - (z - z0)/(z1 - z0) clipped by
+    z0/z1, z = |p_{i+1}-p_{i-1}| / |p_{i+2}-p_{i-2}|, then the minimum with the
+    upstream neighbour by the sign of the pressure difference -- with one
+    correction taken from Colella & Woodward (1984), eq. A.1-A.2, the method it
+    cites: flattening applies only where the pressure jump is strong
+    (|dp|/min(p) > delta) *and* the flow is compressive (u_{i-1} > u_{i+1});
+    elsewhere chi_bar = 1.  (As written, ppm.py:124 sets chi_bar = 0 -- full
+    flattening -- exactly where the flow is neither, which would drop smooth
+    flow to first order.)  Parity unpinned.
     """
     P = wS[..., 4]
     dp1 = gather(P, 1, bc) - gather(P, -1, bc)
@@ -62,9 +70,9 @@ def flatten_coefficient(wS, axis, bc, delta=.33, z0=.75, z1=.85):
     chi_bar[z > z1] = 0
     chi_bar[z < z0] = 1
     vn = wS[..., axis + 1]
-    compress = (gather(vn, -1, bc) - gather(vn, 1, bc)) <= 0
+    not_compressive = (gather(vn, -1, bc) - gather(vn, 1, bc)) <= 0
     weak = divide(np.abs(dp1), np.minimum(gather(P, 1, bc), gather(P, -1, bc))) <= delta
-    chi_bar[compress & weak] = 0
+    chi_bar[not_compressive | weak] = 1
     sgn = np.sign(dp1)
     chi = np.copy(chi_bar)
     lo = sgn < 0

@@ -73,10 +73,13 @@ def artificial_viscosity(wS, qf, axis, cfg):
 
     The reference's ``apply_artificial_viscosity`` (ppm.py:138-170) cannot
     run in 2D (it adds arrays of shapes (N+2,N) and (N,N)) and its result is
-    never used.  This follows its coefficient
-    ``nu = min(1, (dx*lambda)^2 / (beta c_min^2)) * lambda`` for compressive
-    faces, with lambda the face velocity divergence including the transverse
-    term of eq. 35, applied to conserved differences.  Parity unpinned.
+    never used.  This follows the paper it cites: lambda is h times the face
+    velocity divergence (the normal velocity difference plus the quarter-sum of
+    the transverse differences, eq. 35), nu = min(1, lambda^2 / (beta c_min^2))
+    * lambda on compressive faces (eq. 36) and the viscous flux acts on the
+    conserved differences (eq. 38).  ppm.py:157 multiplies lambda by dx once
+    more, which makes the coefficient vanish as the grid is refined; that extra
+    factor is left out.  Parity unpinned.
     """
     bc, g = cfg.bc, cfg.gamma
     vn = wS[..., axis + 1]
@@ -88,7 +91,7 @@ def artificial_viscosity(wS, qf, axis, cfg):
     with np.errstate(invalid="ignore"):
         cs = np.sqrt(fv.divide(g * wS[..., 4], wS[..., 0]))
     cmin = np.minimum(cs, fv.gather(cs, 1, bc))
-    nu = np.minimum(1, fv.divide((cfg.dx * lam) ** 2, cfg.av_beta * cmin ** 2)) * lam
+    nu = np.minimum(1, fv.divide(lam ** 2, cfg.av_beta * cmin ** 2)) * lam
     nu[lam >= 0] = 0
     return cfg.av_alpha * (nu[..., None] * (fv.gather(qf, 1, bc) - qf))
 

@@ -54,6 +54,11 @@ def test_create_rejects_bad_config_before_touching_the_gpu():
     assert L.astrea_create(ctypes.byref(bad), ctypes.byref(h)) == -1
     bad = _lib.Cfg(dim=1, n0=64, n1=1, model=3, precision=16, gamma=1.4, dx=1.0, cfl=.5, t_end=1.0, checkpoints=1)
     assert L.astrea_create(ctypes.byref(bad), ctypes.byref(h)) == -1
+    # PPM flattening with constrained transport
+    bad = RunConfig(dim=2, n0=64, n1=64, model=8, scheme="ppm", solver="hlld", magnetic_2d=True, flatten=True).to_c()
+    assert bad.flags == 2 | 4
+    assert L.astrea_create(ctypes.byref(bad), ctypes.byref(h)) == -1
+    assert b"flattening" in L.astrea_last_error()
     assert L.astrea_step(None, None, 1, None) == -6
 
 

@@ -44,7 +44,7 @@ sys.path.insert(0, ROOT)
 
 SEED = 20261203
 METRIC = "cell-updates/s FP32-batched vs FP64 plain (L1<=1e-5); serve p50/p99 ms"
-WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc)+HLLC+SSPRK3, CFL 0.8"
+WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc) with flattening and artificial viscosity + HLLC + SSPRK3, CFL 0.8"
 # DRAM bytes (read + write) of one stage-0 sweep launch of the headline FP32
 # workload, measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum)
 SWEEP_DRAM_BYTES = 103.7e6
@@ -70,7 +70,8 @@ def run_config(n, precision):
     # iteration position, star momentum always in component 1, f_plus for sL > 0) loses
     # positivity on this flow within a few steps; the arithmetic per cell is the same
     return RunConfig(dim=2, n0=n, n1=n, model=4, precision=precision, scheme="ppm", solver="hllc",
-                     integrator="ssprk33", boundary="wrap", gamma=1.4, dx=1.0 / n, cfl=0.8, t_end=1.0, compat=False)
+                     integrator="ssprk33", boundary="wrap", gamma=1.4, dx=1.0 / n, cfl=0.8, t_end=1.0, compat=False,
+                     flatten=True, viscosity=True)
 
 
 class ClockSampler:
@@ -145,7 +146,8 @@ def cpu_sample_worker(args):
     sys.path.insert(0, ROOT)
     from oracle import stepper
     cfg = stepper.OracleConfig(dim=2, scheme="ppm", solver="hllc", integrator="ssprk33", gamma=1.4, bc="wrap",
-                               dx=1.0 / n, cfl=0.8, eig="analytic", t_end=1.0, compat=False)
+                               dx=1.0 / n, cfl=0.8, eig="analytic", t_end=1.0, compat=False, flatten=True,
+                               viscosity=True)
     q = stepper.initialise(shear_layer(n, seed), cfg)
     t, idx, order = 0.0, 1, [0, 1]
     t0 = time.perf_counter()
@@ -417,7 +419,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "cells": cells, "precision": "fp32 (FP64 pressure recovery)",
-                       "hllc": "textbook (flag PHYSICAL)", "parallelism": f"replicas x{ws}",
+                       "hllc": "textbook (flag PHYSICAL)",
+                       "flattening_viscosity": "flags FLATTEN|VISCOSITY; the reference's code for both fails when "
+                                               "called, formulas per the cited papers (parity unpinned)",
+                       "parallelism": f"replicas x{ws}",
                        "l2": "working set 5 x 67 MB > L2: inputs larger than L2"},
             "fp64_plain": {"value": value64, "unit": "cell-updates/s", "steps": args.fp64_steps,
                            "ms_per_step": ms64 / args.fp64_steps},

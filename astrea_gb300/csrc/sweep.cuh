@@ -102,13 +102,16 @@ template <int SCH, int DIM, int TS, int TT, int NV> struct Smem {
   // In 2D the viscous fluxes sit where the final fluxes go (they are added there),
   // and the coefficients in the gap of region 0 between the staged state and the
   // face arrays; otherwise both go past the end.
+  // The coefficients need chi_bar one column further on each side (n_cb).
   static constexpr int n_eta = SCH == PPM ? G::RH * (G::RW + 1) : 0;
+  static constexpr int n_cb = SCH == PPM ? G::RH * (G::RW + 3) : 0;
   static constexpr int n_mu = SCH == PPM ? NV * TT * G::KW : 0;
   static constexpr bool MU_IN_F = DIM == 2;
-  static constexpr bool ETA_IN_GAP = DIM == 2 && (n_q + n_qw + n_eta <= FA_OFF + n_face);
+  static constexpr bool ETA_IN_GAP = DIM == 2 && (n_q + n_qw + n_eta + n_cb <= FA_OFF + n_face);
   static constexpr int MU_OFF = MU_IN_F ? FA_OFF + n_face : base;
   static constexpr int ETA_OFF = ETA_IN_GAP ? n_q + n_qw : base + (MU_IN_F ? 0 : n_mu);
-  static constexpr int total = base + (MU_IN_F ? 0 : n_mu) + (ETA_IN_GAP ? 0 : n_eta);
+  static constexpr int CB_OFF = ETA_OFF + n_eta;
+  static constexpr int total = base + (MU_IN_F ? 0 : n_mu) + (ETA_IN_GAP ? 0 : n_eta + n_cb);
 };
 
 template <class M, typename T> __device__ __forceinline__ void load_sm(const T* base, int stride, int idx, T* x) {
@@ -294,33 +297,39 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         return s_w[(pl * G::WH + (rt - (t0 - G::WT))) * G::WW + (x - (s0 + G::W_BEG))];
       };
       if (a.flatten) {
-        constexpr int W = G::RW + 1, H = G::RH;
+        // chi_bar on columns [s0-3, s0+TS+3), then eta on [s0-2, s0+TS+2) from it; each
+        // intermediate is served at a virtual index by its value at the mapped index
+        constexpr int CW = G::RW + 3, EW = G::RW + 1, H = G::RH;
+        constexpr int CB_BEG = G::R_BEG - 2, E_BEG = G::R_BEG - 1;
         constexpr double DZ = 0.85 - 0.75;
-        for (int e = tid; e < W * H; e += nth) {
-          const int row = e / W, col = e % W;
-          const int vx = s0 + G::R_BEG - 1 + col, vt = t0 - G::RT + row;
-          const int x = rs_(vx), rt = DIM == 2 ? rt_(vt) : 0;
-          auto P = [&](int y) -> T { return wv(PP, y, rt); };
-          // chi_bar at real cell y (every difference padded on its own)
-          auto chi_bar = [&](int y) -> T {
-            const T dp1 = P(rs_(y + 1)) - P(rs_(y - 1));
-            const T dp2 = P(rs_(y + 2)) - P(rs_(y - 2));
-            const T z = dvd(abs_(dp1), abs_(dp2));
-            T cb = T(1) - dvd(z - T(.75), T(DZ));
-            if (z > T(.85)) cb = T(0);
-            if (z < T(.75)) cb = T(1);
-            // only strong, compressive pressure jumps are flattened (Colella & Woodward 1984, A.1)
-            const bool not_compressive = (wv(PN, rs_(y - 1), rt) - wv(PN, rs_(y + 1), rt)) <= T(0);
-            const bool weak = dvd(abs_(dp1), npmin(P(rs_(y + 1)), P(rs_(y - 1)))) <= T(.33);
-            if (not_compressive || weak) cb = T(1);
-            return cb;
-          };
-          const T cb = chi_bar(x);
-          const T sgn = npsign(P(rs_(x + 1)) - P(rs_(x - 1)));
+        T* s_cb = sm + S::CB_OFF;
+        for (int e = tid; e < CW * H; e += nth) {
+          const int row = e / CW, col = e % CW;
+          const int y = rs_(s0 + CB_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
+          auto P = [&](int x) -> T { return wv(PP, x, rt); };
+          const T dp1 = P(rs_(y + 1)) - P(rs_(y - 1));
+          const T dp2 = P(rs_(y + 2)) - P(rs_(y - 2));
+          const T z = dvd(abs_(dp1), abs_(dp2));
+          T cb = T(1) - dvd(z - T(.75), T(DZ));
+          if (z > T(.85)) cb = T(0);
+          if (z < T(.75)) cb = T(1);
+          // only strong, compressive pressure jumps are flattened (Colella & Woodward 1984, A.1)
+          const bool not_compressive = (wv(PN, rs_(y - 1), rt) - wv(PN, rs_(y + 1), rt)) <= T(0);
+          const bool weak = dvd(abs_(dp1), npmin(P(rs_(y + 1)), P(rs_(y - 1)))) <= T(.33);
+          if (not_compressive || weak) cb = T(1);
+          s_cb[row * CW + col] = cb;
+        }
+        __syncthreads();
+        for (int e = tid; e < EW * H; e += nth) {
+          const int row = e / EW, col = e % EW;
+          const int x = rs_(s0 + E_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
+          const T* cbrow = s_cb + row * CW - (s0 + CB_BEG);
+          const T cb = cbrow[x];
+          const T sgn = npsign(wv(PP, rs_(x + 1), rt) - wv(PP, rs_(x - 1), rt));
           T chi = cb;
-          if (sgn < T(0)) chi = npmin(cb, chi_bar(rs_(x + 1)));
-          if (sgn > T(0)) chi = npmin(cb, chi_bar(rs_(x - 1)));
-          s_eta[row * W + col] = chi;
+          if (sgn < T(0)) chi = npmin(cb, cbrow[rs_(x + 1)]);
+          if (sgn > T(0)) chi = npmin(cb, cbrow[rs_(x - 1)]);
+          s_eta[row * EW + col] = chi;
         }
       }
       if (a.viscosity) {

@@ -259,11 +259,107 @@ template <typename T> __device__ __forceinline__ T hlld_fast(const T* w, T gamma
 
 template <typename T> __device__ __forceinline__ T pick3(T x0, T x1, T x2, int i) { return i == 0 ? x0 : (i == 1 ? x1 : x2); }
 
+// HLLD as published (Miyoshi & Kusano 2005, eqs. 38-51 and 59-67), used in the
+// physical mode: the reference's solver departs from the paper (sR from
+// min(uL, uR), star momenta without their density factors, the right Alfven
+// speed's sign, momenta in the energy's v.B) and blows up on the Orszag-Tang
+// vortex.  One normal field for both sides: the mean of the two face states'.
+// A star state whose denominator rho (S - u)(S - S_M) - Bn^2 vanishes
+// (relative 1e-10) keeps its transverse velocity and field.
+template <typename T> struct HlldStar { T rs, vs, ws, bys, bzs, Es, vbs; };
+
+template <typename T>
+__device__ void hlld_textbook(int a, T gamma, const T* wp, const T* wm, const T* qp, const T* qm, const T* fp,
+                              const T* fm, T* F) {
+  const int o = (a + 1) % 3, p = (a + 2) % 3;
+  const T Bn = T(.5) * (pick3(wm[5], wm[6], wm[7], a) + pick3(wp[5], wp[6], wp[7], a));
+  const T rL = wm[0], PL = wm[4], rR = wp[0], PR = wp[4];
+  const T uL = pick3(wm[1], wm[2], wm[3], a), vL = pick3(wm[1], wm[2], wm[3], o), wL = pick3(wm[1], wm[2], wm[3], p);
+  const T uR = pick3(wp[1], wp[2], wp[3], a), vR = pick3(wp[1], wp[2], wp[3], o), wR = pick3(wp[1], wp[2], wp[3], p);
+  const T byL = pick3(wm[5], wm[6], wm[7], o), bzL = pick3(wm[5], wm[6], wm[7], p);
+  const T byR = pick3(wp[5], wp[6], wp[7], o), bzR = pick3(wp[5], wp[6], wp[7], p);
+  const T bn2 = Bn * Bn;
+  auto fast = [&](T r, T P, T by, T bz) -> T {
+    const T cs2 = dvd(gamma * P, r);
+    const T ca2 = dvd((bn2 + by * by) + bz * bz, r);
+    const T cx2 = dvd(bn2, r);
+    const T sm = cs2 + ca2;
+    return sqrt_(T(.5) * (sm + sqrt_(npmax(sm * sm - (T(4) * cs2) * cx2, T(0)))));
+  };
+  const T cf = npmax(fast(rL, PL, byL, bzL), fast(rR, PR, byR, bzR));
+  const T sL = npmin(uL, uR) - cf;
+  const T sR = npmax(uL, uR) + cf;
+  const T ptL = PL + T(.5) * ((bn2 + byL * byL) + bzL * bzL);
+  const T ptR = PR + T(.5) * ((bn2 + byR * byR) + bzR * bzR);
+  const T dL = sL - uL, dR = sR - uR;
+  const T den = dR * rR - dL * rL;
+  const T sM = dvd((((dR * rR) * uR - (dL * rL) * uL) - ptR) + ptL, den);
+  const T pts = dvd(((dR * rR) * ptL - (dL * rL) * ptR) + ((rL * rR) * (dR * dL)) * (uR - uL), den);
+  auto star = [&](T r, T u, T v, T w, T by, T bz, T E, T pt, T s, T d) -> HlldStar<T> {
+    HlldStar<T> x;
+    x.rs = r * dvd(d, s - sM);
+    const T rds = (r * d) * (s - sM);
+    const T dn = rds - bn2;
+    const bool degen = abs_(dn) <= T(1e-10) * (abs_(rds) + bn2);
+    const T g = dvd(sM - u, dn);
+    const T fac = dvd((r * d) * d - bn2, dn);
+    x.vs = degen ? v : v - (Bn * by) * g;
+    x.ws = degen ? w : w - (Bn * bz) * g;
+    x.bys = degen ? by : by * fac;
+    x.bzs = degen ? bz : bz * fac;
+    const T vb = (u * Bn + v * by) + w * bz;
+    x.vbs = (sM * Bn + x.vs * x.bys) + x.ws * x.bzs;
+    x.Es = dvd(((d * E - pt * u) + pts * sM) + Bn * (vb - x.vbs), s - sM);
+    return x;
+  };
+  const HlldStar<T> L = star(rL, uL, vL, wL, byL, bzL, qm[4], ptL, sL, dL);
+  const HlldStar<T> R = star(rR, uR, vR, wR, byR, bzR, qp[4], ptR, sR, dR);
+  const T sqL = sqrt_(L.rs), sqR = sqrt_(R.rs);
+  const T ssL = sM - dvd(abs_(Bn), sqL);
+  const T ssR = sM + dvd(abs_(Bn), sqR);
+  const T sg = npsign(Bn);
+  const T d2 = sqL + sqR;
+  const T vss = dvd((sqL * L.vs + sqR * R.vs) + (R.bys - L.bys) * sg, d2);
+  const T wss = dvd((sqL * L.ws + sqR * R.ws) + (R.bzs - L.bzs) * sg, d2);
+  const T byss = dvd((sqL * R.bys + sqR * L.bys) + ((sqL * sqR) * (R.vs - L.vs)) * sg, d2);
+  const T bzss = dvd((sqL * R.bzs + sqR * L.bzs) + ((sqL * sqR) * (R.ws - L.ws)) * sg, d2);
+  const T vbss = (sM * Bn + vss * byss) + wss * bzss;
+  const T EssL = L.Es - (sqL * (L.vbs - vbss)) * sg;
+  const T EssR = R.Es + (sqR * (R.vbs - vbss)) * sg;
+  const bool m1 = (sL <= T(0)) && (T(0) < ssL), m2 = (ssL <= T(0)) && (T(0) < sM);
+  const bool m3 = (sM <= T(0)) && (T(0) < ssR), m4 = (ssR <= T(0)) && (T(0) <= sR), m5 = sR < T(0);
+  // component k of the conserved vector of a (star or double-star) state
+  auto U = [&](int k, T r, T v, T w, T E, T by, T bz) -> T {
+    if (k == 0) return r;
+    if (k == 4) return E;
+    if (k < 4) return k - 1 == a ? r * sM : (k - 1 == o ? r * v : r * w);
+    return k - 5 == a ? Bn : (k - 5 == o ? by : bz);
+  };
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const T usL = U(k, L.rs, L.vs, L.ws, L.Es, L.bys, L.bzs), usR = U(k, R.rs, R.vs, R.ws, R.Es, R.bys, R.bzs);
+    const T ussL = U(k, L.rs, vss, wss, EssL, byss, bzss), ussR = U(k, R.rs, vss, wss, EssR, byss, bzss);
+    const T fsL = fm[k] + (usL - qm[k]) * sL, fsR = fp[k] + (usR - qp[k]) * sR;
+    const T fssL = fsL + (ussL - usL) * ssL, fssR = fsR + (ussR - usR) * ssR;
+    T f = fm[k];
+    if (m1) f = fsL;
+    if (m2) f = fssL;
+    if (m3) f = fssR;
+    if (m4) f = fsR;
+    if (m5) f = fp[k];
+    F[k] = f;
+  }
+}
+
 // HLLD of Miyoshi & Kusano (solvers.py:142-232), reference quirks kept.  Bn is
 // component label+5 of the cell-averaged state right of the interface.
 template <typename T>
 __device__ void hlld(int label, int physical, T gamma, const T* wSr, const T* wp, const T* wm, const T* qp,
                      const T* qm, const T* fp, const T* fm, T* F) {
+  if (physical) {
+    hlld_textbook<T>(label, gamma, wp, wm, qp, qm, fp, fm, F);
+    return;
+  }
   const int a = label, o = label + 1, p = (label + 2) % 3;
   const T rL = wm[0], pL = wm[4], rR = wp[0], pR = wp[4];
   const T uL = pick3(wm[1], wm[2], wm[3], a), uR = pick3(wp[1], wp[2], wp[3], a);

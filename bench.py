@@ -256,10 +256,148 @@ def batched_leg(steps, warmup, ngrids=512, seed=SEED):
     ms = e0.elapsed_time(e1)
     clk = b.clocks()
     done_updates = float(sum((clk["steps"][g] - c_before[g]) * cfgs[g].n0 * cfgs[g].n1 for g in range(ngrids)))
-    return {"value": done_updates / (ms / 1e3), "unit": "cell-updates/s", "grids": ngrids, "cells": cells,
-            "steps": steps, "ms_per_step": ms / steps, "non_finite_grids": int((clk["status"] != 0).sum()),
-            "workload": "512 four-quadrant Riemann grids 128^2..1024^2, PLM+LLF/PPM+HLLC 50/50, FP32, edge, CFL 0.8",
-            "graph": "one CUDA graph per step, persistent sweep kernels over a tile work list"}
+    out = {"value": done_updates / (ms / 1e3), "unit": "cell-updates/s", "grids": ngrids, "cells": cells,
+           "steps": steps, "ms_per_step": ms / steps, "non_finite_grids": int((clk["status"] != 0).sum()),
+           "workload": "512 four-quadrant Riemann grids 128^2..1024^2, PLM+LLF/PPM+HLLC 50/50, FP32, edge, CFL 0.8",
+           "graph": "one CUDA graph per step, persistent sweep kernels over a tile work list"}
+    del b
+    torch.cuda.empty_cache()
+    out["fp64_check"] = batched_fp64_check(cfgs, seeds, warmup + steps)
+    return out
+
+
+def batched_fp64_check(cfgs, seeds, steps, count=32):
+    """Per-instance FP32-vs-FP64 L1(rho) of the first ``count`` batched grids after ``steps`` steps."""
+    import torch
+    from dataclasses import replace
+    from astrea_gb300.batch import Batch
+    from astrea_gb300.serving import Request
+    sub = cfgs[:count]
+    out = {}
+    for prec in (32, 64):
+        b = Batch([replace(c, precision=prec) for c in sub])
+        for g, c in enumerate(sub):
+            r = Request(rid=g, arrival=0.0, dim=2, n=4, mhd=False, scheme="plm", solver="llf", t_end=.25,
+                        seed=seeds[g])
+            q4 = torch.as_tensor(r.initial_state(), dtype=torch.float64, device="cuda")
+            w = q4[[0, 2]][:, [0, 2]].repeat_interleave(c.n0 // 2, 0).repeat_interleave(c.n1 // 2, 1)
+            b.initialise_one(g, w)
+        b.step(steps, graph=True)
+        torch.cuda.synchronize()
+        out[prec] = ([b.planes(g)[0].double().clone() for g in range(len(sub))], b.clocks()["status"])
+        del b
+    l1 = [float(torch.mean(torch.abs(a - d))) for a, d, st32, st64 in
+          zip(out[32][0], out[64][0], out[32][1], out[64][1]) if st32 == 0 and st64 == 0 and torch.isfinite(a).all()]
+    return {"instances": len(sub), "finite_in_both": len(l1), "steps": steps,
+            "l1_rho_median": float(np.median(l1)) if l1 else None, "l1_rho_max": float(np.max(l1)) if l1 else None}
+
+
+def orszag_tang(n):
+    """Point primitives of the periodic Orszag-Tang vortex on [0,1]^2 (gamma = 5/3)."""
+    x = (np.arange(n) + .5) / n
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    w = np.zeros((n, n, 8))
+    w[..., 0] = 25.0 / (36.0 * np.pi)
+    w[..., 4] = 5.0 / (12.0 * np.pi)
+    w[..., 1] = -np.sin(2 * np.pi * Y)
+    w[..., 2] = np.sin(2 * np.pi * X)
+    w[..., 5] = -np.sin(2 * np.pi * Y) / np.sqrt(4 * np.pi)
+    w[..., 6] = np.sin(4 * np.pi * X) / np.sqrt(4 * np.pi)
+    return w
+
+
+def div_b(state, dx):
+    """Central-difference div B of the cell-averaged field (periodic), on the device: (mean |.|, max |.|)."""
+    import torch
+    bx, by = state[5].double(), state[6].double()
+    d = (torch.roll(bx, -1, 0) - torch.roll(bx, 1, 0)) / (2 * dx) + (torch.roll(by, -1, 1) - torch.roll(by, 1, 1)) / (2 * dx)
+    return float(d.abs().mean()), float(d.abs().max())
+
+
+def mhd_leg(n, steps):
+    """Orszag-Tang 1024^2, WENO5 + HLLD + SSPRK3, CFL 0.4: FP32 rate, L1(rho) vs FP64, div B."""
+    import torch
+    from astrea_gb300.solver import RunConfig, Solver
+    w = orszag_tang(n)
+
+    def cfg(prec):
+        return RunConfig(dim=2, n0=n, n1=n, model=8, precision=prec, scheme="weno5", solver="hlld",
+                         integrator="ssprk33", boundary="wrap", gamma=5.0 / 3.0, dx=1.0 / n, cfl=0.4, t_end=0.5,
+                         compat=False)
+    res = {}
+    for prec in (32, 64):
+        s = Solver(cfg(prec))
+        s.initialise(w)
+        s.reset_clock()
+        if prec == 32:
+            res["div_b_initial"] = div_b(s.state, 1.0 / n)[0]
+        s.step(2, graph=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        s.step(steps, graph=True)
+        e1.record()
+        torch.cuda.synchronize()
+        res[prec] = {"rate": n * n * steps / (e0.elapsed_time(e1) / 1e3), "rho": s.state[0].double().clone(),
+                     "div_b": div_b(s.state, 1.0 / n), "clock": s.clock()}
+        del s
+        torch.cuda.empty_cache()
+    l1 = float(torch.mean(torch.abs(res[32]["rho"] - res[64]["rho"])))
+    return {"workload": f"Orszag-Tang {n}^2 periodic, WENO5 + HLLD (published form, flag PHYSICAL) + SSPRK3, CFL 0.4, "
+                        f"cell-centred B (the reference's constrained transport with an HLL-type solver goes "
+                        f"non-finite near t=0.19 on this vortex, in the oracle too)",
+            "steps": steps + 2, "t": res[32]["clock"]["t"],
+            "fp32": {"value": res[32]["rate"], "unit": "cell-updates/s"},
+            "fp64": {"value": res[64]["rate"], "unit": "cell-updates/s"},
+            "l1_rho_fp32_vs_fp64": l1,
+            "div_b": {"initial_mean_abs": res["div_b_initial"], "fp32_mean_abs": res[32]["div_b"][0],
+                      "fp32_max_abs": res[32]["div_b"][1], "fp64_mean_abs": res[64]["div_b"][0],
+                      "fp64_max_abs": res[64]["div_b"][1],
+                      "form": "central difference of cell-averaged B (the reference has no div B diagnostic)"},
+            "status": [int(res[32]["clock"]["status"]), int(res[64]["clock"]["status"])]}
+
+
+def sod_cfg(n):
+    from astrea_gb300.solver import RunConfig
+    return RunConfig(dim=1, n0=n, model=3, precision=64, scheme="plm", solver="llf", integrator="ssprk33",
+                     boundary="edge", gamma=1.4, dx=1.0 / n, cfl=0.8, t_end=0.2)
+
+
+def sod_point(n):
+    w = np.zeros((n, 8))
+    w[: n // 2, 0], w[: n // 2, 4] = 1.0, 1.0
+    w[n // 2:, 0], w[n // 2:, 4] = .125, .1
+    return w
+
+
+def sod_leg(n=4096):
+    """The plain method (FP64, reference quirks kept) on the 1D Sod problem to t = 0.2 through Solver.run."""
+    import torch
+    from astrea_gb300.solver import Solver
+    s = Solver(sod_cfg(n))
+    s.initialise(sod_point(n))
+    s.reset_clock()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    clk = s.run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"workload": f"1D Sod N={n}, PLM-minmod + LLF + SSPRK3, CFL 0.8, to t=0.2, FP64 plain",
+            "steps": int(clk["steps"]), "t": clk["t"], "ms": ms, "value": n * clk["steps"] / (ms / 1e3),
+            "unit": "cell-updates/s"}, s.conservative().cpu().numpy()
+
+
+def sod_oracle(n=4096):
+    """CPU baseline of the Sod workload (the oracle to t = 0.2, one core) and its final state."""
+    from oracle import stepper
+    oc = stepper.OracleConfig(dim=1, scheme="plm", solver="llf", integrator="ssprk33", gamma=1.4, bc="edge",
+                              dx=1.0 / n, cfl=0.8, eig="analytic", t_end=0.2)
+    t0 = time.perf_counter()
+    q, t, steps, _dts = stepper.run(stepper.initialise(sod_point(n), oc), oc)
+    wall = time.perf_counter() - t0
+    return q, t, steps, wall
 
 
 def serving_leg(count, rate, seed=SEED):
@@ -287,6 +425,9 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--mhd-n", type=int, default=1024)
+    ap.add_argument("--mhd-steps", type=int, default=20)
+    ap.add_argument("--sod-n", type=int, default=4096)
     ap.add_argument("--cpu-n", type=int, default=256)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
@@ -399,14 +540,24 @@ def main():
     del s32
     torch.cuda.empty_cache()
 
-    batched = serving = None
+    batched = serving = mhd = sod = sod_state = None
     if not args.no_extras:
         batched = batched_leg(args.batch_steps, 2)
         torch.cuda.empty_cache()
         serving = serving_leg(args.serve_requests, args.serve_rate)
         torch.cuda.empty_cache()
+        mhd = mhd_leg(args.mhd_n, args.mhd_steps)
+        torch.cuda.empty_cache()
+        sod, sod_state = sod_leg(args.sod_n)
 
     cpu = None
+    if rank == 0 and not args.no_cpu and sod is not None:
+        q, t_o, steps_o, wall = sod_oracle(args.sod_n)
+        sod["cpu_baseline"] = {"value": args.sod_n * steps_o / wall, "unit": "cell-updates/s", "cores": 1,
+                               "kind": "port", "sample": f"the whole run ({steps_o} steps), oracle, 1 core"}
+        sod["steps_oracle"] = steps_o
+        sod["rel_err_vs_oracle"] = float(np.max(np.abs(sod_state - q)) / np.max(np.abs(q)))
+        sod["l1_rho_vs_oracle"] = float(np.mean(np.abs(sod_state[:, 0] - q[:, 0])))
     if rank == 0 and not args.no_cpu:
         v, cores = cpu_baseline(args.cpu_n, 1, args.cpu_steps)
         cpu = {"value": v, "unit": "cell-updates/s", "cores": cores, "kind": "port",
@@ -436,6 +587,8 @@ def main():
                     "d2h_bytes_per_step": state_bytes, "steps": args.e2e_steps},
             "batched": batched,
             "serving": serving,
+            "mhd_orszag_tang": mhd,
+            "sod_1d": sod,
             "clocks": cs.summary(),
             "cpu_baseline": cpu,
             "t_simulated": clk32["t"],

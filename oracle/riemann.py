@@ -84,6 +84,99 @@ def _fast_speed_bx(w, gamma, normal=0):
         return np.sqrt(.5 * (cs ** 2 + ca ** 2 + np.sqrt(((cs ** 2 + ca ** 2) ** 2) - (4 * (cs ** 2) * (cax ** 2)))))
 
 
+def hlld_textbook(a, gamma, Bn, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus):
+    """HLLD as published (Miyoshi & Kusano 2005, eqs. 38-51 and 59-67); not the reference's solver.
+
+    The reference's calculate_HLLD_flux (solvers.py:142-232) departs from the
+    paper in ways that make it blow up on the Orszag-Tang vortex within a few
+    dozen steps: sR uses min(uL, uR), the star and double-star momenta are
+    missing their density factors, the right Alfven speed has the wrong sign and
+    the energy uses momenta in place of velocities.  This is the paper's solver,
+    with one normal field ``Bn`` shared by both sides (the caller passes the mean
+    of the two face states' normal fields).  A star state
+    whose denominator rho (S - u)(S - S_M) - Bn^2 vanishes (relative 1e-10)
+    keeps its transverse velocity and field (the paper's degenerate case).
+    """
+    o, p = (a + 1) % 3, (a + 2) % 3
+    rL, uL, vL, wL, PL = w_minus[..., 0], w_minus[..., 1 + a], w_minus[..., 1 + o], w_minus[..., 1 + p], w_minus[..., 4]
+    rR, uR, vR, wR, PR = w_plus[..., 0], w_plus[..., 1 + a], w_plus[..., 1 + o], w_plus[..., 1 + p], w_plus[..., 4]
+    byL, bzL, byR, bzR = w_minus[..., 5 + o], w_minus[..., 5 + p], w_plus[..., 5 + o], w_plus[..., 5 + p]
+    bn2 = Bn * Bn
+    with np.errstate(invalid="ignore", divide="ignore"):
+        def fast(r, P, by, bz):
+            cs2 = divide(gamma * P, r)
+            ca2 = divide((bn2 + by * by) + bz * bz, r)
+            cx2 = divide(bn2, r)
+            sm = cs2 + ca2
+            return np.sqrt(.5 * (sm + np.sqrt(np.maximum(sm * sm - (4 * cs2) * cx2, 0.))))
+        cf = np.maximum(fast(rL, PL, byL, bzL), fast(rR, PR, byR, bzR))
+        sL = np.minimum(uL, uR) - cf
+        sR = np.maximum(uL, uR) + cf
+        ptL = PL + .5 * ((bn2 + byL * byL) + bzL * bzL)
+        ptR = PR + .5 * ((bn2 + byR * byR) + bzR * bzR)
+        dL, dR = sL - uL, sR - uR
+        den = dR * rR - dL * rL
+        sM = divide((((dR * rR) * uR - (dL * rL) * uL) - ptR) + ptL, den)
+        pts = divide(((dR * rR) * ptL - (dL * rL) * ptR) + ((rL * rR) * (dR * dL)) * (uR - uL), den)
+
+        def star(r, u, v, w, by, bz, E, pt, s, d):
+            rs = r * divide(d, s - sM)
+            rds = (r * d) * (s - sM)
+            dn = rds - bn2
+            degen = np.abs(dn) <= 1e-10 * (np.abs(rds) + bn2)
+            g = divide(sM - u, dn)
+            fac = divide((r * d) * d - bn2, dn)
+            vs = np.where(degen, v, v - (Bn * by) * g)
+            ws = np.where(degen, w, w - (Bn * bz) * g)
+            bys = np.where(degen, by, by * fac)
+            bzs = np.where(degen, bz, bz * fac)
+            vb = (u * Bn + v * by) + w * bz
+            vbs = (sM * Bn + vs * bys) + ws * bzs
+            Es = divide(((d * E - pt * u) + pts * sM) + Bn * (vb - vbs), s - sM)
+            return rs, vs, ws, bys, bzs, Es, vbs
+
+        rsL, vsL, wsL, bysL, bzsL, EsL, vbsL = star(rL, uL, vL, wL, byL, bzL, q_minus[..., 4], ptL, sL, dL)
+        rsR, vsR, wsR, bysR, bzsR, EsR, vbsR = star(rR, uR, vR, wR, byR, bzR, q_plus[..., 4], ptR, sR, dR)
+        sqL, sqR = np.sqrt(rsL), np.sqrt(rsR)
+        ssL = sM - divide(np.abs(Bn), sqL)
+        ssR = sM + divide(np.abs(Bn), sqR)
+        sg = np.sign(Bn)
+        d2 = sqL + sqR
+        vss = divide((sqL * vsL + sqR * vsR) + (bysR - bysL) * sg, d2)
+        wss = divide((sqL * wsL + sqR * wsR) + (bzsR - bzsL) * sg, d2)
+        byss = divide((sqL * bysR + sqR * bysL) + ((sqL * sqR) * (vsR - vsL)) * sg, d2)
+        bzss = divide((sqL * bzsR + sqR * bzsL) + ((sqL * sqR) * (wsR - wsL)) * sg, d2)
+        vbss = (sM * Bn + vss * byss) + wss * bzss
+        EssL = EsL - (sqL * (vbsL - vbss)) * sg
+        EssR = EsR + (sqR * (vbsR - vbss)) * sg
+
+    def vec(r, v, w, E, by, bz, like):
+        U = np.zeros_like(like)
+        U[..., 0] = r
+        U[..., 1 + a] = r * sM
+        U[..., 1 + o] = r * v
+        U[..., 1 + p] = r * w
+        U[..., 4] = E
+        U[..., 5 + a] = Bn
+        U[..., 5 + o] = by
+        U[..., 5 + p] = bz
+        return U
+
+    UsL = vec(rsL, vsL, wsL, EsL, bysL, bzsL, q_minus)
+    UsR = vec(rsR, vsR, wsR, EsR, bysR, bzsR, q_plus)
+    UssL = vec(rsL, vss, wss, EssL, byss, bzss, q_minus)
+    UssR = vec(rsR, vss, wss, EssR, byss, bzss, q_plus)
+    FsL = f_minus + (UsL - q_minus) * sL[..., None]
+    FsR = f_plus + (UsR - q_plus) * sR[..., None]
+    FssL = FsL + (UssL - UsL) * ssL[..., None]
+    FssR = FsR + (UssR - UsR) * ssR[..., None]
+    F = np.copy(f_minus)
+    for m, G in (((sL <= 0) & (0 < ssL), FsL), ((ssL <= 0) & (0 < sM), FssL), ((sM <= 0) & (0 < ssR), FssR),
+                 ((ssR <= 0) & (0 <= sR), FsR), (sR < 0, f_plus)):
+        F[m] = G[m]
+    return F
+
+
 def hlld(label, gamma, wS_right, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus, physical=False):
     """HLLD of Miyoshi & Kusano (solvers.py:142-232), reference quirks kept.
 
@@ -91,8 +184,13 @@ def hlld(label, gamma, wS_right, w_plus, w_minus, q_plus, q_minus, f_plus, f_min
     interface (``add_boundary(wS)[1:]``, solvers.py:168); its component
     ``label+5`` is the normal field used in the star and double-star states.
     ``physical=True`` (not in the reference): ``label`` is the physical sweep
-    axis and the fast speed uses the normal field B[label].
+    axis and the solver is the published one (``hlld_textbook``) with the mean
+    of the two face states' normal fields as B_n.
     """
+    if physical:
+        a = label % 3
+        Bn = .5 * (w_minus[..., 5 + a] + w_plus[..., 5 + a])
+        return hlld_textbook(a, gamma, Bn, w_plus, w_minus, q_plus, q_minus, f_plus, f_minus)
     a, o, p = label % 3, (label + 1) % 3, (label + 2) % 3
     rL, vL, pL, BL, QL = w_minus[..., 0], w_minus[..., 1:4], w_minus[..., 4], w_minus[..., 5:8], q_minus
     rR, vR, pR, BR, QR = w_plus[..., 0], w_plus[..., 1:4], w_plus[..., 4], w_plus[..., 5:8], q_plus

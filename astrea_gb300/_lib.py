@@ -16,6 +16,7 @@ EXPORTS = [
     "astrea_version", "astrea_last_error", "astrea_create", "astrea_destroy", "astrea_layout", "astrea_initialise",
     "astrea_reset_clock", "astrea_step", "astrea_graph_step", "astrea_get_clock", "astrea_space", "astrea_time",
     "astrea_to_primitive", "astrea_reduce_conserved", "astrea_step_timed", "astrea_reduce_conserved_static",
+    "astrea_sweep_tile",
 ]
 
 
@@ -66,6 +67,7 @@ def load(path=LIB_PATH):
             "astrea_to_primitive": ([vp, vp, vp, vp], i),
             "astrea_reduce_conserved": ([vp, vp, dp, vp], i),
             "astrea_reduce_conserved_static": ([vp, i, ctypes.c_longlong, i, dp, vp], i),
+            "astrea_sweep_tile": ([vp, i, ip, ip], i),
             "astrea_step_timed": ([vp, vp, i, dp, ip, vp], i),
         }
         for name, (args, res) in sig.items():

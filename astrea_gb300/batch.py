@@ -35,6 +35,8 @@ _SIGS = {
     "astrea_batch_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "astrea_batch_graph_step": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "astrea_batch_clocks": ([ctypes.c_void_p] * 7, ctypes.c_int),
+    "astrea_batch_tile": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+                          ctypes.c_int),
 }
 
 
@@ -114,6 +116,15 @@ class SlotBatch:
         fn = self.lib.astrea_batch_graph_step if graph else self.lib.astrea_batch_step
         _lib.check(fn(self.handle, ctypes.c_void_p(self.arena.data_ptr()), int(n), _stream()))
 
+    def tiles(self):
+        """The (cells along, rows across) tile of each axis's batched sweep (tuned at the first step)."""
+        out = []
+        for ax in range(self.dim):
+            ts, tt = ctypes.c_int(), ctypes.c_int()
+            _lib.check(self.lib.astrea_batch_tile(self.handle, ax, ctypes.byref(ts), ctypes.byref(tt)))
+            out.append((ts.value, tt.value))
+        return out
+
     def clocks(self):
         g = self.max_slots
         t, dt = (ctypes.c_double * g)(), (ctypes.c_double * g)()
@@ -173,6 +184,9 @@ class Batch:
 
     def clocks(self):
         return self.sb.clocks()
+
+    def tiles(self):
+        return self.sb.tiles()
 
     def run(self, max_steps=None, check_every=16, graph=True):
         n = 0

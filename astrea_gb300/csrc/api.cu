@@ -12,7 +12,10 @@
 // graph serves even and odd steps.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -94,7 +97,17 @@ struct IEngine {
   virtual int initialise(const void* prim, void* out, cudaStream_t st) = 0;
   virtual int to_primitive(const void* state, void* out, cudaStream_t st) = 0;
   virtual int reduce(const void* state, double* host, cudaStream_t st) = 0;
+  // pick the sweep tile of each axis (once, before the first step; not during a capture)
+  virtual int tune(const void* state, cudaStream_t st) = 0;
+  virtual void tile_of(int ax, int* ts, int* tt) const = 0;
 };
+
+// Sweep-tile autotuner: per (precision, model, scheme, solver, flags, grid size,
+// device, axis) the fastest candidate tile, timed once on the grid itself and
+// shared by every handle with the same key.  ASTREA_SWEEP_TILE=<index> forces a
+// candidate (where it is built).
+static std::mutex g_tune_mutex;
+static std::map<std::string, int> g_tune_cache;
 
 struct astrea_handle {
   IEngine* eng;
@@ -107,6 +120,9 @@ template <typename T> struct Engine final : IEngine {
   T* wf[2] = {nullptr, nullptr};  // 2D MHD: face values of each sweep
   T* ez = nullptr;                // 2D MHD: corner electric field
   SweepFn<T> sweep[2] = {nullptr, nullptr};
+  SweepFn<T> cand[2][NTILES2] = {};  // tile candidates per axis (nullptr: not built for this configuration)
+  int tile[2] = {0, 0};
+  bool tuned = false;
 
   ~Engine() override {
     for (int i = 0; i < 2; ++i) { cudaFree(k[i]); cudaFree(d[i]); cudaFree(wf[i]); }
@@ -132,7 +148,7 @@ template <typename T> struct Engine final : IEngine {
         return fail(ASTREA_ERR_OOM, "constrained-transport buffer allocation failed");
       CK(cudaFuncSetAttribute(corner_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corner_smem_bytes<T>()));
     }
-    SweepFn<T> (*getter)(int, int, int, int) = nullptr;
+    SweepFn<T> (*getter)(int, int, int, int, int) = nullptr;
     switch (cfg.scheme) {
       case PCM: getter = &get_sweep<T, PCM>; break;
       case PLM: getter = &get_sweep<T, PLM>; break;
@@ -142,14 +158,81 @@ template <typename T> struct Engine final : IEngine {
       case WENO7: getter = &get_sweep<T, WENO7>; break;
       default: return fail(ASTREA_ERR_CONFIG, "unknown scheme");
     }
-    sweep[0] = getter(cfg.model, cfg.solver, cfg.dim, 0);
-    if (cfg.dim == 2) sweep[1] = getter(cfg.model, cfg.solver, cfg.dim, 1);
+    for (int ax = 0; ax < cfg.dim; ++ax)
+      for (int t = 0; t < NTILES2; ++t) cand[ax][t] = getter(cfg.model, cfg.solver, cfg.dim, ax, t);
+    sweep[0] = cand[0][0];
+    sweep[1] = cfg.dim == 2 ? cand[1][0] : nullptr;
     if (!sweep[0] || (cfg.dim == 2 && !sweep[1]))
       return fail(ASTREA_ERR_CONFIG, "no kernel for this (model, solver, dimension); use model 8 for HLLD or transverse velocities");
     // set the kernels' shared-memory attribute now, outside any stream capture
     SweepArgs<T> probe{};
     probe.n0 = 0;
-    for (int i = 0; i < cfg.dim; ++i) CK(sweep[i](probe, nullptr));
+    for (int ax = 0; ax < cfg.dim; ++ax)
+      for (int t = 0; t < NTILES2; ++t)
+        if (cand[ax][t]) CK(cand[ax][t](probe, nullptr));
+    return ASTREA_OK;
+  }
+
+  void tile_of(int ax, int* ts, int* tt) const override {
+    const int t = tile[ax & 1];
+    if (cfg.dim == 1) { *ts = TS1; *tt = 1; }
+    else if (t == 0) { *ts = Tile2<0>::TS; *tt = Tile2<0>::TT; }
+    else { *ts = Tile2<1>::TS; *tt = Tile2<1>::TT; }
+  }
+
+  int tune(const void* state, cudaStream_t st) override {
+    if (tuned) return ASTREA_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return ASTREA_OK;  // keep the default tile inside a capture
+    tuned = true;
+    const char* env = std::getenv("ASTREA_SWEEP_TILE");
+    const int forced = (env && env[0] >= '0' && env[0] <= '9') ? std::atoi(env) : -1;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    for (int ax = 0; ax < cfg.dim; ++ax) {
+      int n_cand = 0;
+      for (int t = 0; t < NTILES2; ++t) n_cand += cand[ax][t] != nullptr;
+      if (forced >= 0 && forced < NTILES2 && cand[ax][forced]) { tile[ax] = forced; sweep[ax] = cand[ax][forced]; continue; }
+      if (n_cand < 2) continue;
+      char key[160];
+      std::snprintf(key, sizeof(key), "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", (int)sizeof(T), cfg.model, cfg.scheme, cfg.solver,
+                    cfg.flags, cfg.n0, cfg.n1, cfg.boundary, dev, ax);
+      {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) { tile[ax] = it->second; sweep[ax] = cand[ax][it->second]; continue; }
+      }
+      // time each candidate: the axis's first sweep (store the divergence) on this grid's state
+      Clock* c = clk + 1;
+      CK(cudaMemsetAsync(&c->done, 0, sizeof(int), st));
+      SweepArgs<T> a = base_args(static_cast<const T*>(state), c);
+      a.mode = 0;
+      a.want_emax = 0;
+      a.dout = d[ax];
+      cudaEvent_t e0, e1;
+      CK(cudaEventCreate(&e0));
+      CK(cudaEventCreate(&e1));
+      float best = 0.f;
+      int best_t = 0;
+      for (int t = 0; t < NTILES2; ++t) {
+        if (!cand[ax][t]) continue;
+        CK(cand[ax][t](a, st));
+        CK(cudaEventRecord(e0, st));
+        for (int r = 0; r < 3; ++r) CK(cand[ax][t](a, st));
+        CK(cudaEventRecord(e1, st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (t == 0 || ms < best) { best = ms; best_t = t; }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      tile[ax] = best_t;
+      sweep[ax] = cand[ax][best_t];
+      std::lock_guard<std::mutex> lock(g_tune_mutex);
+      g_tune_cache[key] = best_t;
+    }
     return ASTREA_OK;
   }
 
@@ -476,6 +559,8 @@ int astrea_reset_clock(astrea_handle* h, double t, int idx, int order, void* str
 int astrea_step(astrea_handle* h, void* state, int nsteps, void* stream) {
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int trc = h->eng->tune(state, st);
+  if (trc) return trc;
   for (int i = 0; i < nsteps; ++i) {
     int rc = h->eng->enqueue_step(state, h->eng->clk, true, st);
     if (rc) return rc;
@@ -486,6 +571,8 @@ int astrea_step(astrea_handle* h, void* state, int nsteps, void* stream) {
 int astrea_step_timed(astrea_handle* h, void* state, int nsteps, double* kernel_ms, int* launches, void* stream) {
   if (!h || !state || !kernel_ms || !launches) return fail(ASTREA_ERR_ARG, "NULL argument");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int trc = h->eng->tune(state, st);
+  if (trc) return trc;
   KTimer tm;
   for (int i = 0; i < nsteps; ++i) {
     int rc = h->eng->enqueue_step(state, h->eng->clk, true, st, &tm);
@@ -509,6 +596,8 @@ int astrea_graph_step(astrea_handle* h, void* state, int nsteps, void* stream) {
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
   IEngine* e = h->eng;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int trc = e->tune(state, st);
+  if (trc) return trc;
   if (!e->graph || e->graph_state != state) {
     if (e->graph) {
       cudaGraphExecDestroy(e->graph);
@@ -549,6 +638,8 @@ int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* d
 int astrea_space(astrea_handle* h, const void* state, int order, void* flux_ax0, void* flux_ax1, double* eigmax,
                  void* stream) {
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
+  int trc = h->eng->tune(state, static_cast<cudaStream_t>(stream));
+  if (trc) return trc;
   return h->eng->space(state, order & 1, flux_ax0, flux_ax1, eigmax, static_cast<cudaStream_t>(stream));
 }
 
@@ -556,6 +647,8 @@ int astrea_time(astrea_handle* h, void* state, double dt, int order, void* strea
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
   IEngine* e = h->eng;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int trc = e->tune(state, st);
+  if (trc) return trc;
   Clock c;
   std::memset(&c, 0, sizeof(c));
   c.t = 0.0;
@@ -577,6 +670,12 @@ int astrea_time(astrea_handle* h, void* state, double dt, int order, void* strea
 int astrea_to_primitive(astrea_handle* h, const void* state, void* prim_out, void* stream) {
   if (!h || !state || !prim_out) return fail(ASTREA_ERR_ARG, "NULL argument");
   return h->eng->to_primitive(state, prim_out, static_cast<cudaStream_t>(stream));
+}
+
+int astrea_sweep_tile(const astrea_handle* h, int axis, int* ts, int* tt) {
+  if (!h || !ts || !tt || axis < 0 || axis > 1) return fail(ASTREA_ERR_ARG, "bad argument");
+  h->eng->tile_of(axis, ts, tt);
+  return ASTREA_OK;
 }
 
 int astrea_reduce_conserved(astrea_handle* h, const void* state, double* sums_host, void* stream) {

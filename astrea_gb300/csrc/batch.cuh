@@ -49,8 +49,9 @@ template <int MID, int DIM, int TS, int TT, typename T> constexpr size_t batch_s
   return (size_t)(m > c ? m : c);
 }
 
-template <typename T, int MID, int DIM, int AX, int TS, int TT>
-__global__ void __launch_bounds__(256, (SweepOcc<T, MID, 256>::value)) batched_sweep_kernel(const BatchArgs<T> b) {
+template <typename T, int MID, int DIM, int AX, int TS, int TT, int NT>
+__global__ void __launch_bounds__((NT > 256 ? NT : 256), (SweepOcc<T, MID, (NT > 256 ? NT : 256)>::value))
+    batched_sweep_kernel(const BatchArgs<T> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;
   constexpr int HLL = MID == 8 ? HLLD : HLLC;
@@ -88,12 +89,12 @@ __global__ void __launch_bounds__(256, (SweepOcc<T, MID, 256>::value)) batched_s
     a.out = out + gd.base;
     a.clock = clk;
     switch (gd.combo) {
-      case C_PLM_LLF: sweep_tile<T, MID, PLM, LLF, DIM, AX, TS, TT>(a, w.s0, w.t0, smem_raw); break;
-      case C_PLM_HLL: sweep_tile<T, MID, PLM, HLL, DIM, AX, TS, TT>(a, w.s0, w.t0, smem_raw); break;
-      case C_PPM_LLF: sweep_tile<T, MID, PPM, LLF, DIM, AX, TS, TT>(a, w.s0, w.t0, smem_raw); break;
-      case C_PPM_HLL: sweep_tile<T, MID, PPM, HLL, DIM, AX, TS, TT>(a, w.s0, w.t0, smem_raw); break;
-      case C_WENO5_LLF: sweep_tile<T, MID, WENO5, LLF, DIM, AX, TS, TT>(a, w.s0, w.t0, smem_raw); break;
-      default: sweep_tile<T, MID, WENO5, HLL, DIM, AX, TS, TT>(a, w.s0, w.t0, smem_raw); break;
+      case C_PLM_LLF: sweep_tile<T, MID, PLM, LLF, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
+      case C_PLM_HLL: sweep_tile<T, MID, PLM, HLL, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
+      case C_PPM_LLF: sweep_tile<T, MID, PPM, LLF, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
+      case C_PPM_HLL: sweep_tile<T, MID, PPM, HLL, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
+      case C_WENO5_LLF: sweep_tile<T, MID, WENO5, LLF, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
+      default: sweep_tile<T, MID, WENO5, HLL, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
     }
   }
 }

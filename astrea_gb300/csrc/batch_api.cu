@@ -7,6 +7,7 @@
 // slot by one of its own time steps: one persistent kernel per sweep walks a
 // work list of tiles of all occupied slots (largest grids first).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -19,14 +20,17 @@ using namespace astrea;
 namespace astrea {
 ASTREA_EXTERN_BATCH(float)
 ASTREA_EXTERN_BATCH(double)
+ASTREA_EXTERN_BATCH_T16
 }  // namespace astrea
 
-template <typename T> static BatchFn<T> batched_for(int model, int dim, int ax) {
-  return dim == 1 ? get_batched<T, 1>(model, ax) : get_batched<T, 2>(model, ax);
+template <typename T> static BatchFn<T> batched_for(int model, int dim, int ax, int v) {
+  return dim == 1 ? get_batched<T, 1>(model, ax, v) : get_batched<T, 2>(model, ax, v);
 }
-template <typename T> static int occupancy_for(int model, int dim, int ax) {
-  return dim == 1 ? get_occupancy<T, 1>(model, ax) : get_occupancy<T, 2>(model, ax);
+template <typename T> static int occupancy_for(int model, int dim, int ax, int v) {
+  return dim == 1 ? get_occupancy<T, 1>(model, ax, v) : get_occupancy<T, 2>(model, ax, v);
 }
+static int tile_ts(int dim, int v) { return dim == 1 ? BTS1 : (v == 0 ? BTile2<0>::TS : BTile2<1>::TS); }
+static int tile_tt(int dim, int v) { return dim == 1 ? 1 : (v == 0 ? BTile2<0>::TT : BTile2<1>::TT); }
 
 namespace {
 
@@ -79,6 +83,10 @@ struct IBatch {
   virtual int rebuild() = 0;
   virtual int enqueue_step(void* arena, cudaStream_t st) = 0;
   virtual int initialise(int slot, const void* prim, void* arena, cudaStream_t st) = 0;
+  // pick each axis's tile (once, at the first step with occupied slots; not during a capture)
+  virtual int tune(void* arena, cudaStream_t st) = 0;
+  int var[2] = {0, 0};
+  bool tuned = false;
 };
 
 struct astrea_batch {
@@ -88,9 +96,9 @@ struct astrea_batch {
 template <typename T> struct Batch final : IBatch {
   T *k0 = nullptr, *k1 = nullptr, *d0 = nullptr, *d1 = nullptr, *tmp = nullptr;
   BGrid<T>* d_grids = nullptr;
-  BatchFn<T> sweep[2] = {nullptr, nullptr};
+  BatchFn<T> cand[2][NBTILES2] = {};  // tile candidates per axis (nullptr: not built)
+  int occ_c[2][NBTILES2] = {};
   int nctas[2] = {0, 0};
-  int occ[2] = {1, 1};
   int sms = 152;
 
   ~Batch() override {
@@ -109,12 +117,65 @@ template <typename T> struct Batch final : IBatch {
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     for (int ax = 0; ax < dim; ++ax) {
-      sweep[ax] = batched_for<T>(model, dim, ax);
-      if (!sweep[ax]) return fail(ASTREA_ERR_CONFIG, "no batched kernel for this model/dimension");
-      BatchArgs<T> probe{};
-      CK(sweep[ax](probe, 0, nullptr));
-      occ[ax] = std::max(1, occupancy_for<T>(model, dim, ax));
+      for (int v = 0; v < NBTILES2; ++v) {
+        cand[ax][v] = batched_for<T>(model, dim, ax, v);
+        if (!cand[ax][v]) continue;
+        BatchArgs<T> probe{};
+        CK(cand[ax][v](probe, 0, nullptr));
+        occ_c[ax][v] = std::max(1, occupancy_for<T>(model, dim, ax, v));
+      }
+      if (!cand[ax][0]) return fail(ASTREA_ERR_CONFIG, "no batched kernel for this model/dimension");
     }
+    return ASTREA_OK;
+  }
+
+  // Batch tile autotuner: time the first sweep of each axis (store the divergence;
+  // no clock update) over the current work list for every built tile and keep the
+  // fastest.  ASTREA_BATCH_TILE=<index> forces a tile (where it is built).
+  int tune(void* arena, cudaStream_t st) override {
+    if (tuned) return ASTREA_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return ASTREA_OK;
+    if (std::find(active.begin(), active.end(), 1) == active.end()) return ASTREA_OK;
+    tuned = true;
+    const char* env = std::getenv("ASTREA_BATCH_TILE");
+    const int forced = (env && env[0] >= '0' && env[0] <= '9') ? std::atoi(env) : -1;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    for (int ax = 0; ax < dim; ++ax) {
+      if (forced >= 0 && forced < NBTILES2 && cand[ax][forced]) { var[ax] = forced; continue; }
+      float best = 0.f;
+      int best_v = 0;
+      for (int v = 0; v < NBTILES2; ++v) {
+        if (!cand[ax][v]) continue;
+        var[ax] = v;
+        int rc = rebuild();
+        if (rc) return rc;
+        BatchArgs<T> b = args(static_cast<T*>(arena));
+        b.stage = 0;
+        b.mode = 0;
+        b.want_emax = 0;
+        b.dout_sel = ax;
+        rc = launch_sweep(b, ax, 15, st);
+        if (rc) return rc;
+        CK(cudaEventRecord(e0, st));
+        for (int r = 0; r < 2; ++r) {
+          rc = launch_sweep(b, ax, 15, st);
+          if (rc) return rc;
+        }
+        CK(cudaEventRecord(e1, st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (v == 0 || ms < best) { best = ms; best_v = v; }
+      }
+      var[ax] = best_v;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dirty = true;
     return ASTREA_OK;
   }
 
@@ -142,7 +203,7 @@ template <typename T> struct Batch final : IBatch {
     auto cells = [&](int s) { return (long long)host_grids[s].n0 * (dim == 2 ? host_grids[s].n1 : 1); };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells(x) > cells(y); });
     for (int ax = 0; ax < dim; ++ax) {
-      const int TS = dim == 1 ? BTS1 : BTS2, TT = dim == 1 ? 1 : BTT2;
+      const int TS = tile_ts(dim, var[ax]), TT = tile_tt(dim, var[ax]);
       std::vector<BItem> it;
       for (int g : order) {
         const astrea_grid& a = host_grids[g];
@@ -159,7 +220,7 @@ template <typename T> struct Batch final : IBatch {
         CK(cudaMalloc(&items[ax], sizeof(BItem) * items_cap[ax]));
       }
       if (!it.empty()) CK(cudaMemcpy(items[ax], it.data(), sizeof(BItem) * it.size(), cudaMemcpyHostToDevice));
-      nctas[ax] = std::max(1, std::min(nitems[ax], occ[ax] * sms));
+      nctas[ax] = std::max(1, std::min(nitems[ax], occ_c[ax][var[ax]] * sms));
     }
     dirty = false;
     return ASTREA_OK;
@@ -184,7 +245,7 @@ template <typename T> struct Batch final : IBatch {
     b.nitems = nitems[ax];
     b.counter = counters + slot;
     CK(cudaMemsetAsync(counters + slot, 0, sizeof(int), st));
-    CK(sweep[ax](b, nctas[ax], st));
+    CK(cand[ax][var[ax]](b, nctas[ax], st));
     return ASTREA_OK;
   }
 
@@ -208,7 +269,7 @@ template <typename T> struct Batch final : IBatch {
     dt_kernel<<<(max_slots + 127) / 128, 128, 0, st>>>(clocks, max_slots);
     CK(cudaGetLastError());
     if (nitems[0] > 0) {
-      const int TS = dim == 1 ? BTS1 : BTS2, TT = dim == 1 ? 1 : BTT2;
+      const int TS = tile_ts(dim, var[0]), TT = tile_tt(dim, var[0]);
       batched_combine0_kernel<T><<<nitems[0], 256, 0, st>>>(b, items[0], nv, dim == 2, ns == 1, TS, TT);
       CK(cudaGetLastError());
     }
@@ -351,8 +412,17 @@ int astrea_batch_initialise(astrea_batch* h, int slot, const void* prim_arena, v
   return h->b->initialise(slot, prim_arena, arena, static_cast<cudaStream_t>(stream));
 }
 
+int astrea_batch_tile(const astrea_batch* h, int axis, int* ts, int* tt) {
+  if (!h || !ts || !tt || axis < 0 || axis > 1) return fail(ASTREA_ERR_ARG, "bad argument");
+  *ts = tile_ts(h->b->dim, h->b->var[axis]);
+  *tt = tile_tt(h->b->dim, h->b->var[axis]);
+  return ASTREA_OK;
+}
+
 int astrea_batch_step(astrea_batch* h, void* arena, int nsteps, void* stream) {
   if (!h || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
+  int trc = h->b->tune(arena, static_cast<cudaStream_t>(stream));
+  if (trc) return trc;
   for (int i = 0; i < nsteps; ++i) {
     int rc = h->b->enqueue_step(arena, static_cast<cudaStream_t>(stream));
     if (rc) return rc;
@@ -364,6 +434,8 @@ int astrea_batch_graph_step(astrea_batch* h, void* arena, int nsteps, void* stre
   if (!h || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
   IBatch* b = h->b;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int trc = b->tune(arena, st);
+  if (trc) return trc;
   if (b->dirty || !b->graph || b->graph_arena != arena) {
     if (b->graph) {
       cudaGraphExecDestroy(b->graph);

@@ -1,5 +1,5 @@
 // Batched sweep kernels: float, 2D, model 8 axis 1.
 #include "batch_launch.cuh"
 namespace astrea {
-ASTREA_BATCH_INST(float, 8, 2, 1)
+ASTREA_BATCH_INST(float, 8, 2, 1, 0)
 }

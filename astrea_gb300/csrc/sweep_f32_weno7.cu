@@ -1,5 +1,5 @@
 // Sweep kernels for precision float, scheme WENO7 (one translation unit per pair).
 #include "sweep_launch.cuh"
 namespace astrea {
-template SweepFn<float> get_sweep<float, WENO7>(int, int, int, int);
+template SweepFn<float> get_sweep<float, WENO7>(int, int, int, int, int);
 }

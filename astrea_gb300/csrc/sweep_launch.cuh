@@ -8,19 +8,23 @@ namespace astrea {
 
 template <typename T> using SweepFn = cudaError_t (*)(const SweepArgs<T>&, cudaStream_t);
 
-// tiles: 1D 32 cells x 64 threads; 2D 32 (sweep) x 8 (rows) x 256 threads
+// Tiles: 1D 32 cells x 64 threads.  2D candidates, picked per grid by the
+// engine's autotuner: 32 (sweep) x 8 (rows) x 256 threads, and 32 x 16 x 512
+// threads (fewer transverse halo rows per cell, same threads per SM; FP32
+// Euler tiles only, whose shared memory and 64 registers allow it).
 constexpr int TS1 = 32, NT1 = 64;
-constexpr int TS2 = 32, TT2 = 8, NT2 = 256;
+constexpr int NTILES2 = 2;
+template <int I> struct Tile2;
+template <> struct Tile2<0> { static constexpr int TS = 32, TT = 8, NT = 256; };
+template <> struct Tile2<1> { static constexpr int TS = 32, TT = 16, NT = 512; };
 
-template <typename T, int MID, int SCH, int DIM> constexpr size_t sweep_smem_bytes() {
-  constexpr int TS = DIM == 1 ? TS1 : TS2, TT = DIM == 1 ? 1 : TT2;
+template <typename T, int MID, int SCH, int DIM, int TS, int TT> constexpr size_t sweep_smem_bytes() {
   return sizeof(T) * (size_t)Smem<SCH, DIM, TS, TT, Model<MID>::NV>::total;
 }
 
-template <typename T, int MID, int SCH, int SOL, int DIM, int AX>
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT>
 cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
-  constexpr int TS = DIM == 1 ? TS1 : TS2, TT = DIM == 1 ? 1 : TT2, NT = DIM == 1 ? NT1 : NT2;
-  constexpr size_t bytes = sweep_smem_bytes<T, MID, SCH, DIM>();
+  constexpr size_t bytes = sweep_smem_bytes<T, MID, SCH, DIM, TS, TT>();
   static_assert(bytes <= 227 * 1024, "sweep tile exceeds the shared memory of one CTA");
   auto k = sweep_kernel<T, MID, SCH, SOL, DIM, AX, TS, TT, NT>;
   int dev = 0;
@@ -40,37 +44,51 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// launcher of one (model, scheme, solver, dimension, axis) for tile candidate ``tile``; nullptr if that
+// tile is not built for it
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX> SweepFn<T> sweep_for_tile(int tile) {
+  if constexpr (DIM == 1) {
+    return tile == 0 ? &launch_sweep<T, MID, SCH, SOL, 1, 0, TS1, 1, NT1> : nullptr;
+  } else {
+    if (tile == 0) return &launch_sweep<T, MID, SCH, SOL, 2, AX, Tile2<0>::TS, Tile2<0>::TT, Tile2<0>::NT>;
+    if constexpr (sizeof(T) == 4 && MID != 8) {
+      if (tile == 1) return &launch_sweep<T, MID, SCH, SOL, 2, AX, Tile2<1>::TS, Tile2<1>::TT, Tile2<1>::NT>;
+    }
+    return nullptr;
+  }
+}
+
 // Supported (model, solver) pairs: Euler models with LLF/HLLC, the 8-variable
 // model with LLF/HLLC/HLLD.
-template <typename T, int SCH> SweepFn<T> get_sweep(int mid, int sol, int dim, int ax) {
+template <typename T, int SCH> SweepFn<T> get_sweep(int mid, int sol, int dim, int ax, int tile) {
   if (dim == 1) {
     if (mid == 3) {
-      if (sol == LLF) return &launch_sweep<T, 3, SCH, LLF, 1, 0>;
-      if (sol == HLLC) return &launch_sweep<T, 3, SCH, HLLC, 1, 0>;
+      if (sol == LLF) return sweep_for_tile<T, 3, SCH, LLF, 1, 0>(tile);
+      if (sol == HLLC) return sweep_for_tile<T, 3, SCH, HLLC, 1, 0>(tile);
     } else if (mid == 8) {
-      if (sol == LLF) return &launch_sweep<T, 8, SCH, LLF, 1, 0>;
-      if (sol == HLLC) return &launch_sweep<T, 8, SCH, HLLC, 1, 0>;
-      if (sol == HLLD) return &launch_sweep<T, 8, SCH, HLLD, 1, 0>;
+      if (sol == LLF) return sweep_for_tile<T, 8, SCH, LLF, 1, 0>(tile);
+      if (sol == HLLC) return sweep_for_tile<T, 8, SCH, HLLC, 1, 0>(tile);
+      if (sol == HLLD) return sweep_for_tile<T, 8, SCH, HLLD, 1, 0>(tile);
     }
   } else if (dim == 2) {
     if (mid == 4) {
-      if (sol == LLF) return ax == 0 ? &launch_sweep<T, 4, SCH, LLF, 2, 0> : &launch_sweep<T, 4, SCH, LLF, 2, 1>;
-      if (sol == HLLC) return ax == 0 ? &launch_sweep<T, 4, SCH, HLLC, 2, 0> : &launch_sweep<T, 4, SCH, HLLC, 2, 1>;
+      if (sol == LLF) return ax == 0 ? sweep_for_tile<T, 4, SCH, LLF, 2, 0>(tile) : sweep_for_tile<T, 4, SCH, LLF, 2, 1>(tile);
+      if (sol == HLLC) return ax == 0 ? sweep_for_tile<T, 4, SCH, HLLC, 2, 0>(tile) : sweep_for_tile<T, 4, SCH, HLLC, 2, 1>(tile);
     } else if (mid == 8) {
-      if (sol == LLF) return ax == 0 ? &launch_sweep<T, 8, SCH, LLF, 2, 0> : &launch_sweep<T, 8, SCH, LLF, 2, 1>;
-      if (sol == HLLC) return ax == 0 ? &launch_sweep<T, 8, SCH, HLLC, 2, 0> : &launch_sweep<T, 8, SCH, HLLC, 2, 1>;
-      if (sol == HLLD) return ax == 0 ? &launch_sweep<T, 8, SCH, HLLD, 2, 0> : &launch_sweep<T, 8, SCH, HLLD, 2, 1>;
+      if (sol == LLF) return ax == 0 ? sweep_for_tile<T, 8, SCH, LLF, 2, 0>(tile) : sweep_for_tile<T, 8, SCH, LLF, 2, 1>(tile);
+      if (sol == HLLC) return ax == 0 ? sweep_for_tile<T, 8, SCH, HLLC, 2, 0>(tile) : sweep_for_tile<T, 8, SCH, HLLC, 2, 1>(tile);
+      if (sol == HLLD) return ax == 0 ? sweep_for_tile<T, 8, SCH, HLLD, 2, 0>(tile) : sweep_for_tile<T, 8, SCH, HLLD, 2, 1>(tile);
     }
   }
   return nullptr;
 }
 
 #define ASTREA_EXTERN_GET_SWEEP(T)                                               \
-  extern template SweepFn<T> get_sweep<T, PCM>(int, int, int, int);              \
-  extern template SweepFn<T> get_sweep<T, PLM>(int, int, int, int);              \
-  extern template SweepFn<T> get_sweep<T, PPM>(int, int, int, int);              \
-  extern template SweepFn<T> get_sweep<T, WENO3>(int, int, int, int);            \
-  extern template SweepFn<T> get_sweep<T, WENO5>(int, int, int, int);            \
-  extern template SweepFn<T> get_sweep<T, WENO7>(int, int, int, int);
+  extern template SweepFn<T> get_sweep<T, PCM>(int, int, int, int, int);              \
+  extern template SweepFn<T> get_sweep<T, PLM>(int, int, int, int, int);              \
+  extern template SweepFn<T> get_sweep<T, PPM>(int, int, int, int, int);              \
+  extern template SweepFn<T> get_sweep<T, WENO3>(int, int, int, int, int);            \
+  extern template SweepFn<T> get_sweep<T, WENO5>(int, int, int, int, int);            \
+  extern template SweepFn<T> get_sweep<T, WENO7>(int, int, int, int, int);
 
 }  // namespace astrea

@@ -223,6 +223,15 @@ class Solver:
         _lib.check(self.lib.astrea_time(self.handle, ctypes.c_void_p(self.state.data_ptr()), float(dt), int(order),
                                         _stream()))
 
+    def sweep_tiles(self):
+        """The (cells along, rows across) tile of each axis's sweep kernel (tuned at the first step)."""
+        out = []
+        for ax in range(self.cfg.dim):
+            ts, tt = ctypes.c_int(), ctypes.c_int()
+            _lib.check(self.lib.astrea_sweep_tile(self.handle, ax, ctypes.byref(ts), ctypes.byref(tt)))
+            out.append((ts.value, tt.value))
+        return out
+
     def conserved_sums(self):
         """Neumaier-compensated FP64 sums of the stored variables."""
         out = (ctypes.c_double * self.nv)()

@@ -259,6 +259,7 @@ def batched_leg(steps, warmup, ngrids=512, seed=SEED):
     clk = b.clocks()
     done_updates = float(sum((clk["steps"][g] - c_before[g]) * cfgs[g].n0 * cfgs[g].n1 for g in range(ngrids)))
     out = {"value": done_updates / (ms / 1e3), "unit": "cell-updates/s", "grids": ngrids, "cells": cells,
+           "tiles": b.tiles(),
            "steps": steps, "ms_per_step": ms / steps, "non_finite_grids": int((clk["status"] != 0).sum()),
            "workload": "512 four-quadrant Riemann grids 128^2..1024^2, PLM+LLF/PPM+HLLC 50/50, FP32, edge, CFL 0.8",
            "graph": "one CUDA graph per step, persistent sweep kernels over a tile work list"}
@@ -471,6 +472,7 @@ def main():
     barrier(ws)
     value = ws * cells * args.steps / (ms / 1e3)
     clk32 = s32.clock()
+    tiles32 = s32.sweep_tiles()
 
     # roofline of the sweep kernel: algorithmic bytes per launch / mean launch time.
     # Per step: stage 0 two sweeps read the state and write a divergence (2*C*s per cell each);
@@ -577,7 +579,8 @@ def main():
                        "flattening_viscosity": "flags FLATTEN|VISCOSITY; the reference's code for both fails when "
                                                "called, formulas per the cited papers (parity unpinned)",
                        "parallelism": f"replicas x{ws}",
-                       "l2": "working set 5 x 67 MB > L2: inputs larger than L2"},
+                       "l2": "working set 5 x 67 MB > L2: inputs larger than L2",
+                       "sweep_tiles": tiles32, "tiles_from": "autotuner (timed on the grid at the first step)"},
             "fp64_plain": {"value": value64, "unit": "cell-updates/s", "steps": args.fp64_steps,
                            "ms_per_step": ms64 / args.fp64_steps},
             "fp32_over_fp64": value / ws / value64,

@@ -128,6 +128,12 @@ int astrea_graph_step(astrea_handle* h, void* state, int nsteps, void* stream);
  * measurement; no counterpart in the reference.) */
 int astrea_step_timed(astrea_handle* h, void* state, int nsteps, double* kernel_ms, int* launches, void* stream);
 
+/* The sweep tile in use along ``axis`` (cells along the sweep x rows across it).
+ * 2D grids pick theirs among the built candidates by timing them on the grid
+ * at the first step (the environment variable ASTREA_SWEEP_TILE=<index> forces
+ * one).  No counterpart in the reference. */
+int astrea_sweep_tile(const astrea_handle* h, int axis, int* ts, int* tt);
+
 /* Read the device clock (synchronises ``stream``).  status bit 0: a
  * non-finite wave speed or dt was seen. */
 int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* done, int* status, void* stream);
@@ -211,6 +217,12 @@ void astrea_batch_destroy(astrea_batch* b);
 int astrea_batch_set(astrea_batch* b, int slot, const astrea_grid* grid, long long offset);
 /* Release ``slot`` (its grid is no longer advanced). */
 int astrea_batch_clear(astrea_batch* b, int slot);
+/* The tile in use along ``axis`` (cells along the sweep x rows across it).  A
+ * batch picks it among the built candidates by timing them on its work list at
+ * its first step (ASTREA_BATCH_TILE=<index> forces one).  No counterpart in the
+ * reference. */
+int astrea_batch_tile(const astrea_batch* h, int axis, int* ts, int* tt);
+
 /* Point primitives -> cell-averaged conservatives for one slot; ``prim_arena``
  * holds the primitives at the slot's offset. */
 int astrea_batch_initialise(astrea_batch* b, int slot, const void* prim_arena, void* arena, void* stream);

@@ -41,6 +41,10 @@ static int stages_of(int integ) {
     case SSPRK22: return 2;
     case SSPRK33: return 3;
     case SSPRK43: return 4;
+    case SSPRK53: return 5;
+    case SSPRK54: return 5;
+    case SSPRK104: return 11;  // the reference's (10,4) evaluates the operator 11 times
+    case RK4: return 4;
     default: return -1;
   }
 }
@@ -120,12 +124,14 @@ template <typename T> struct Engine final : IEngine {
   T* wf[2] = {nullptr, nullptr};  // 2D MHD: face values of each sweep
   T* ez = nullptr;                // 2D MHD: corner electric field
   SweepFn<T> sweep[2] = {nullptr, nullptr};
+  T* reg[6] = {};                    // registers of the integrators with more live stages (rk_stage_kernel)
   SweepFn<T> cand[2][NTILES2] = {};  // tile candidates per axis (nullptr: not built for this configuration)
   int tile[2] = {0, 0};
   bool tuned = false;
 
   ~Engine() override {
     for (int i = 0; i < 2; ++i) { cudaFree(k[i]); cudaFree(d[i]); cudaFree(wf[i]); }
+    for (T* r : reg) cudaFree(r);
     cudaFree(tmp);
     cudaFree(ez);
   }
@@ -141,6 +147,11 @@ template <typename T> struct Engine final : IEngine {
       if (cudaMalloc(&d[i], bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "divergence buffer allocation failed");
     }
     if (cudaMalloc(&tmp, bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "scratch allocation failed");
+    if (cfg.integrator >= SSPRK53) {
+      const int nreg = cfg.integrator == SSPRK53 ? 6 : (cfg.integrator == SSPRK104 ? 3 : (cfg.integrator == RK4 ? 4 : 5));
+      for (int i = 0; i < nreg; ++i)
+        if (cudaMalloc(&reg[i], bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "register allocation failed");
+    }
     if (ct()) {
       const size_t b8 = sizeof(T) * 8 * (size_t)cells;
       if (cudaMalloc(&wf[0], b8) != cudaSuccess || cudaMalloc(&wf[1], b8) != cudaSuccess ||
@@ -310,8 +321,76 @@ template <typename T> struct Engine final : IEngine {
     return ASTREA_OK;
   }
 
+  // input state of stage s of the register integrators
+  const T* rk_input(int s, const T* u) const {
+    if (s == 0) return u;
+    switch (cfg.integrator) {
+      case RK4: return reg[0];
+      case SSPRK53:
+      case SSPRK54: return reg[s - 1];
+      default: return s <= 5 ? reg[0] : (s == 6 ? reg[1] : reg[2]);  // SSPRK104
+    }
+  }
+  // destination register of stage s (the state at the last stage)
+  T* rk_output(int s, T* u) const {
+    if (s == stages_of(cfg.integrator) - 1) return u;
+    switch (cfg.integrator) {
+      case RK4: return reg[0];
+      case SSPRK53:
+      case SSPRK54: return reg[s];
+      default: return s <= 4 ? reg[0] : (s == 5 ? reg[1] : reg[2]);  // SSPRK104
+    }
+  }
+
+  // SSP-RK (5,3), (5,4), (10,4), RK4: both sweeps of a stage store their divergences,
+  // then one element-wise kernel forms L and the stage's register.
+  int enqueue_step_rk(T* u, Clock* c, bool device_dt, cudaStream_t st, KTimer* tm) {
+    const int ns = stages_of(cfg.integrator);
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>((cells + threads - 1) / threads, 152LL * 16);
+    for (int s = 0; s < ns; ++s) {
+      SweepArgs<T> a = base_args(rk_input(s, u), c);
+      a.mode = 0;
+      a.want_emax = s == 0;
+      for (int ax = 0; ax < cfg.dim; ++ax) {
+        a.dout = d[ax];
+        TSTART(0);
+        CK(sweep[ax](a, st));
+        TSTOP();
+      }
+      if (s == 0 && device_dt) {
+        TSTART(2);
+        dt_kernel<<<1, 32, 0, st>>>(c, 1);
+        CK(cudaGetLastError());
+        TSTOP();
+      }
+      RkStage<T> r{};
+      r.u = u;
+      for (int i = 0; i < 6; ++i) r.r[i] = reg[i];
+      r.d0 = d[0];
+      r.d1 = cfg.dim == 2 ? d[1] : nullptr;
+      r.out = rk_output(s, u);
+      r.n = (long long)nv * plane();
+      r.integ = cfg.integrator;
+      r.stage = s;
+      r.clk = c;
+      TSTART(1);
+      rk_stage_kernel<T><<<blocks, threads, 0, st>>>(r);
+      CK(cudaGetLastError());
+      TSTOP();
+    }
+    if (device_dt) {
+      TSTART(2);
+      end_step_kernel<<<1, 32, 0, st>>>(c, 1);
+      CK(cudaGetLastError());
+      TSTOP();
+    }
+    return ASTREA_OK;
+  }
+
   int enqueue_step(void* state, Clock* c, bool device_dt, cudaStream_t st, KTimer* tm = nullptr) override {
     T* u = static_cast<T*>(state);
+    if (cfg.integrator >= SSPRK53) return enqueue_step_rk(u, c, device_dt, st, tm);
     const int ns = stages_of(cfg.integrator);
     if (ns < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this build");
     if (ct()) return enqueue_step_ct(u, c, device_dt, st, tm);
@@ -467,6 +546,8 @@ static int validate(const astrea_cfg* c) {
   if (c->boundary != EDGE && c->boundary != WRAP) return fail(ASTREA_ERR_CONFIG, "boundary must be edge(0) or wrap(1)");
   if ((c->flags & ASTREA_FLAG_CT) && (c->dim != 2 || c->model != 8))
     return fail(ASTREA_ERR_CONFIG, "constrained transport needs dim 2 and model 8");
+  if ((c->flags & ASTREA_FLAG_CT) && c->integrator >= SSPRK53)
+    return fail(ASTREA_ERR_CONFIG, "constrained transport runs with Euler and SSP-RK (2,2), (3,3), (4,3)");
   if ((c->flags & ASTREA_FLAG_CT) && (c->flags & ASTREA_FLAG_FLATTEN) && c->scheme == PPM)
     return fail(ASTREA_ERR_CONFIG, "PPM flattening is not available with constrained transport");
   if (!(c->dx > 0) || !(c->cfl > 0) || !(c->gamma > 1) || c->checkpoints < 1)

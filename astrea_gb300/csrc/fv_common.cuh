@@ -14,7 +14,7 @@ namespace astrea {
 enum Scheme { PCM = 0, PLM = 1, PPM = 2, WENO3 = 3, WENO5 = 4, WENO7 = 5 };
 enum Solver { LLF = 0, HLLC = 1, HLLD = 2 };
 enum Boundary { EDGE = 0, WRAP = 1 };
-enum Integrator { EULER = 0, SSPRK22 = 1, SSPRK33 = 2, SSPRK43 = 3 };
+enum Integrator { EULER = 0, SSPRK22 = 1, SSPRK33 = 2, SSPRK43 = 3, SSPRK53 = 4, SSPRK54 = 5, SSPRK104 = 6, RK4 = 7 };
 
 // ---------------------------------------------------------------- precision traits
 template <typename T> struct Prec;

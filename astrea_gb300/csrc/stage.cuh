@@ -23,6 +23,85 @@ __global__ void combine0_kernel(const T* __restrict__ u, const T* __restrict__ d
   }
 }
 
+// One stage of the integrators with more than two live registers
+// (evolvers.py:79-206, SSP-RK (5,3), (5,4), (10,4) and classic RK4), after both
+// sweeps of the stage stored their divergences: L = -(d0 + d1) and the stage
+// formula, with the reference's operation order.  Registers:
+//   RK4      R0 = stage input k, R1..R3 = L0..L2
+//   SSPRK53  R0..R3 = k1..k4, R4 = L0, R5 = L1
+//   SSPRK54  R0..R3 = k1..k4, R4 = L3
+//   SSPRK104 R0 = k (first five stages), R1 = k5, R2 = the second accumulator
+// ``out`` is the stage's destination register (the state itself at the last stage).
+template <typename T> struct RkStage {
+  const T* u;
+  T* r[6];
+  const T* d0;
+  const T* d1;
+  T* out;
+  long long n;
+  int integ, stage;
+  const Clock* clk;
+};
+
+template <typename T> __global__ void rk_stage_kernel(const RkStage<T> a) {
+  if (a.clk->done) return;
+  const T dt = T(a.clk->dt);
+  const int st = a.stage;
+  T* const* R = a.r;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.n; i += (long long)gridDim.x * blockDim.x) {
+    const T L = -(a.d1 ? a.d0[i] + a.d1[i] : a.d0[i]);
+    const T u = a.u[i];
+    T y;
+    switch (a.integ) {
+      case RK4:
+        if (st < 3) {
+          R[1 + st][i] = L;
+          y = u + (st < 2 ? (T(.5) * dt) * L : dt * L);
+        } else {
+          y = u + T(1.0 / 6.0) * (dt * (((R[1][i] + T(2) * R[2][i]) + T(2) * R[3][i]) + L));
+        }
+        break;
+      case SSPRK53: {
+        const T c1 = T(.3772689151171);
+        if (st == 0) { R[4][i] = L; y = u + (c1 * dt) * L; }
+        else if (st == 1) { R[5][i] = L; y = R[0][i] + (c1 * dt) * L; }
+        else if (st == 2) y = (T(.56656131914033) * u + T(.43343868085967) * R[1][i]) + (T(.16352294089771) * dt) * L;
+        else if (st == 3)
+          y = (((T(.09299483444413) * u + T(.0000209036962) * R[0][i]) + T(.90698426185967) * R[2][i])
+               + (T(.00071997378654) * dt) * R[4][i]) + (T(.34217696850008) * dt) * L;
+        else
+          y = (((T(.0073613226092) * u + T(.20127980325145) * R[0][i]) + T(.00182955389682) * R[1][i])
+               + T(.78952932024253) * R[3][i])
+              + (dt * ((T(.0027771981946) * R[4][i] + T(.00001567934613) * R[5][i]) + T(.29786487010104) * L));
+        break;
+      }
+      case SSPRK54:
+        if (st == 0) y = u + (T(.39175222657189) * dt) * L;
+        else if (st == 1) y = (T(.444370493651235) * u + T(.555629506348765) * R[0][i]) + (T(.368410593050371) * dt) * L;
+        else if (st == 2) y = (T(.620101851488403) * u + T(.379898148511597) * R[1][i]) + (T(.251891774271694) * dt) * L;
+        else if (st == 3) {
+          R[4][i] = L;
+          y = (T(.178079954393132) * u + T(.821920045606868) * R[2][i]) + (T(.544974750228521) * dt) * L;
+        } else {
+          y = (((T(.517231671970585) * R[1][i] + T(.096059710526147) * R[2][i]) + (T(.06369246866629) * dt) * R[4][i])
+               + T(.386708617503269) * R[3][i]) + (T(.226007483236906) * dt) * L;
+        }
+        break;
+      default: {  // SSPRK104
+        const T c6 = T(1.0 / 6.0);
+        if (st == 0) y = u + (c6 * dt) * L;
+        else if (st <= 4) y = R[0][i] + (c6 * dt) * L;
+        else if (st == 5) y = (T(3.0 / 5.0) * u + T(6.0 / 15.0) * R[0][i]) + (T(1.0 / 15.0) * dt) * L;
+        else if (st == 6) y = R[1][i] + (c6 * dt) * L;
+        else if (st <= 9) y = R[2][i] + (c6 * dt) * L;
+        else y = ((T(-11.0 / 35.0) * u + T(5.0 / 7.0) * R[1][i]) + T(3.0 / 5.0) * R[2][i]) + (T(1.0 / 10.0) * dt) * L;
+        break;
+      }
+    }
+    a.out[i] = y;
+  }
+}
+
 // dt = cfl * min over axes (in iteration order) of dx / eigmax, clipped to the
 // next checkpoint (astrea.py:70-78).  Python's min keeps the first of equal or
 // unordered values, which decides how a NaN speed propagates.

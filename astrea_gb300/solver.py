@@ -47,8 +47,8 @@ class RunConfig:
     def to_c(self):
         if self.solver not in C.SOLVER or self.solver == "lw":
             raise C.ConfigError(f"solver {self.solver!r} is not provided by the CUDA library")
-        if self.integrator not in ("euler", "ssprk22", "ssprk33", "ssprk43"):
-            raise C.ConfigError(f"integrator {self.integrator!r} is not provided by the CUDA library")
+        if self.magnetic_2d and self.integrator not in ("euler", "ssprk22", "ssprk33", "ssprk43"):
+            raise C.ConfigError("constrained transport runs with Euler and SSP-RK (2,2), (3,3), (4,3)")
         return _lib.Cfg(dim=self.dim, n0=self.n0, n1=self.n1 if self.dim == 2 else 1, model=self.model,
                         precision=self.precision, scheme=C.SCHEME[self.scheme], solver=C.SOLVER[self.solver],
                         integrator=C.INTEGRATOR[self.integrator], boundary=C.BOUNDARY[self.boundary],

@@ -43,7 +43,8 @@ extern "C" {
  * (see astrea_gb300/config.py, mirroring functions/generic.py:159-286) */
 enum astrea_scheme { ASTREA_PCM = 0, ASTREA_PLM = 1, ASTREA_PPM = 2, ASTREA_WENO3 = 3, ASTREA_WENO5 = 4, ASTREA_WENO7 = 5 };
 enum astrea_solver { ASTREA_LLF = 0, ASTREA_HLLC = 1, ASTREA_HLLD = 2 };
-enum astrea_integrator { ASTREA_EULER = 0, ASTREA_SSPRK22 = 1, ASTREA_SSPRK33 = 2, ASTREA_SSPRK43 = 3 };
+enum astrea_integrator { ASTREA_EULER = 0, ASTREA_SSPRK22 = 1, ASTREA_SSPRK33 = 2, ASTREA_SSPRK43 = 3,
+                         ASTREA_SSPRK53 = 4, ASTREA_SSPRK54 = 5, ASTREA_SSPRK104 = 6, ASTREA_RK4 = 7 };
 enum astrea_boundary { ASTREA_EDGE = 0, ASTREA_WRAP = 1 };
 enum astrea_limiter { ASTREA_MINMOD = 0, ASTREA_SUPERBEE = 1 };
 /* stored variables: 3 = 1D Euler (rho, m_x, E); 4 = 2D Euler (rho, m_x, m_y, E);

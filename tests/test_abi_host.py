@@ -114,4 +114,7 @@ def test_runconfig_rejects_unprovided_methods():
     with pytest.raises(C.ConfigError):
         RunConfig(dim=1, n0=64, solver="lw").to_c()
     with pytest.raises(C.ConfigError):
-        RunConfig(dim=1, n0=64, integrator="rk4").to_c()
+        RunConfig(dim=2, n0=64, n1=64, model=8, solver="hlld", integrator="rk4", magnetic_2d=True).to_c()
+    # every integrator of the reference is provided without constrained transport
+    for it in ("euler", "ssprk22", "ssprk33", "ssprk43", "ssprk53", "ssprk54", "ssprk104", "rk4"):
+        assert RunConfig(dim=1, n0=64, integrator=it).to_c().integrator == C.INTEGRATOR[it]

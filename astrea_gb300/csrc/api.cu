@@ -103,6 +103,8 @@ struct IEngine {
   virtual int reduce(const void* state, double* host, cudaStream_t st) = 0;
   // pick the sweep tile of each axis (once, before the first step; not during a capture)
   virtual int tune(const void* state, cudaStream_t st) = 0;
+  // before the first launch on a state pointer (outside a capture): its TMA maps, then tune
+  virtual int prepare(const void* state, cudaStream_t st) = 0;
   virtual void tile_of(int ax, int* ts, int* tt) const = 0;
 };
 
@@ -112,6 +114,44 @@ struct IEngine {
 // candidate (where it is built).
 static std::mutex g_tune_mutex;
 static std::map<std::string, int> g_tune_cache;
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to libcuda)
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// TMA box (x, y) of scheme ``scheme`` for (axis, tile): the kernels' TmaBox
+template <typename T, int SCH> static void box_of(int ax, int tile, cuuint32_t* bw, cuuint32_t* bh) {
+  if (ax == 0) {
+    if (tile == 0) { *bw = TmaBox<T, SCH, 2, 0, 32, 8, 1>::BW; *bh = TmaBox<T, SCH, 2, 0, 32, 8, 1>::BH; }
+    else { *bw = TmaBox<T, SCH, 2, 0, 32, 16, 1>::BW; *bh = TmaBox<T, SCH, 2, 0, 32, 16, 1>::BH; }
+  } else {
+    if (tile == 0) { *bw = TmaBox<T, SCH, 2, 1, 32, 8, 1>::BW; *bh = TmaBox<T, SCH, 2, 1, 32, 8, 1>::BH; }
+    else { *bw = TmaBox<T, SCH, 2, 1, 32, 16, 1>::BW; *bh = TmaBox<T, SCH, 2, 1, 32, 16, 1>::BH; }
+  }
+}
+template <typename T> static void box_for(int scheme, int ax, int tile, cuuint32_t* bw, cuuint32_t* bh) {
+  switch (scheme) {
+    case PCM: box_of<T, PCM>(ax, tile, bw, bh); break;
+    case PLM: box_of<T, PLM>(ax, tile, bw, bh); break;
+    case PPM: box_of<T, PPM>(ax, tile, bw, bh); break;
+    case WENO3: box_of<T, WENO3>(ax, tile, bw, bh); break;
+    case WENO5: box_of<T, WENO5>(ax, tile, bw, bh); break;
+    default: box_of<T, WENO7>(ax, tile, bw, bh); break;
+  }
+}
 
 struct astrea_handle {
   IEngine* eng;
@@ -125,6 +165,10 @@ template <typename T> struct Engine final : IEngine {
   T* ez = nullptr;                // 2D MHD: corner electric field
   SweepFn<T> sweep[2] = {nullptr, nullptr};
   T* reg[6] = {};                    // registers of the integrators with more live stages (rk_stage_kernel)
+  // TMA maps of every buffer a sweep reads (state, stage buffers, registers): 4 per buffer ([axis][tile])
+  static constexpr int kMapSlots = 16;
+  CUtensorMap* d_maps = nullptr;
+  std::vector<const void*> map_ptr;
   SweepFn<T> cand[2][NTILES2] = {};  // tile candidates per axis (nullptr: not built for this configuration)
   int tile[2] = {0, 0};
   bool tuned = false;
@@ -132,6 +176,7 @@ template <typename T> struct Engine final : IEngine {
   ~Engine() override {
     for (int i = 0; i < 2; ++i) { cudaFree(k[i]); cudaFree(d[i]); cudaFree(wf[i]); }
     for (T* r : reg) cudaFree(r);
+    cudaFree(d_maps);
     cudaFree(tmp);
     cudaFree(ez);
   }
@@ -175,6 +220,14 @@ template <typename T> struct Engine final : IEngine {
     sweep[1] = cfg.dim == 2 ? cand[1][0] : nullptr;
     if (!sweep[0] || (cfg.dim == 2 && !sweep[1]))
       return fail(ASTREA_ERR_CONFIG, "no kernel for this (model, solver, dimension); use model 8 for HLLD or transverse velocities");
+    // TMA maps for the engine's own buffers (2D grids whose rows are whole 16-byte units)
+    const char* tma_env = std::getenv("ASTREA_TMA");
+    if (cfg.dim == 2 && ((size_t)cfg.n1 * sizeof(T)) % 16 == 0 && encode_tiled() && !(tma_env && tma_env[0] == '0')) {
+      CK(cudaMalloc(&d_maps, sizeof(CUtensorMap) * 4 * kMapSlots));
+      for (int i = 0; i < 2; ++i) CK(add_map(k[i]));
+      for (T* r : reg)
+        if (r) CK(add_map(r));
+    }
     // set the kernels' shared-memory attribute now, outside any stream capture
     SweepArgs<T> probe{};
     probe.n0 = 0;
@@ -182,6 +235,43 @@ template <typename T> struct Engine final : IEngine {
       for (int t = 0; t < NTILES2; ++t)
         if (cand[ax][t]) CK(cand[ax][t](probe, nullptr));
     return ASTREA_OK;
+  }
+
+  // encode the four TMA maps of a buffer (synchronous; outside any capture)
+  cudaError_t add_map(const void* p) {
+    if (!d_maps || !p || find_map(p) || (int)map_ptr.size() >= kMapSlots) return cudaSuccess;
+    if ((reinterpret_cast<uintptr_t>(p) & 15) != 0) return cudaSuccess;
+    CUtensorMap m[4];
+    const cuuint64_t dims[3] = {(cuuint64_t)cfg.n1, (cuuint64_t)cfg.n0, (cuuint64_t)nv};
+    const cuuint64_t strides[2] = {(cuuint64_t)cfg.n1 * sizeof(T), (cuuint64_t)cells * sizeof(T)};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    for (int ax = 0; ax < 2; ++ax)
+      for (int tile = 0; tile < 2; ++tile) {
+        cuuint32_t box[3] = {0, 0, (cuuint32_t)nv};
+        box_for<T>(cfg.scheme, ax, tile, &box[0], &box[1]);
+        const CUresult r = encode_tiled()(&m[ax * 2 + tile], sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                                                             : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                                          3, const_cast<void*>(p), dims, strides, box, estr,
+                                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return cudaSuccess;  // no map: this buffer is staged with plain loads
+      }
+    cudaError_t e = cudaMemcpy(d_maps + 4 * map_ptr.size(), m, sizeof(m), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    map_ptr.push_back(p);
+    return cudaSuccess;
+  }
+  const CUtensorMap* find_map(const void* p) const {
+    for (size_t i = 0; i < map_ptr.size(); ++i)
+      if (map_ptr[i] == p) return d_maps + 4 * i;
+    return nullptr;
+  }
+
+  int prepare(const void* state, cudaStream_t st) override {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusNone) CK(add_map(state));
+    return tune(state, st);
   }
 
   void tile_of(int ax, int* ts, int* tt) const override {
@@ -266,6 +356,7 @@ template <typename T> struct Engine final : IEngine {
     a.viscosity = (cfg.flags & ASTREA_FLAG_VISCOSITY) ? 1 : 0;
     a.av_alpha = T(0.3);
     a.av_beta = T(0.3);
+    a.tmaps = find_map(q);
     return a;
   }
 
@@ -640,7 +731,7 @@ int astrea_reset_clock(astrea_handle* h, double t, int idx, int order, void* str
 int astrea_step(astrea_handle* h, void* state, int nsteps, void* stream) {
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int trc = h->eng->tune(state, st);
+  int trc = h->eng->prepare(state, st);
   if (trc) return trc;
   for (int i = 0; i < nsteps; ++i) {
     int rc = h->eng->enqueue_step(state, h->eng->clk, true, st);
@@ -652,7 +743,7 @@ int astrea_step(astrea_handle* h, void* state, int nsteps, void* stream) {
 int astrea_step_timed(astrea_handle* h, void* state, int nsteps, double* kernel_ms, int* launches, void* stream) {
   if (!h || !state || !kernel_ms || !launches) return fail(ASTREA_ERR_ARG, "NULL argument");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int trc = h->eng->tune(state, st);
+  int trc = h->eng->prepare(state, st);
   if (trc) return trc;
   KTimer tm;
   for (int i = 0; i < nsteps; ++i) {
@@ -677,7 +768,7 @@ int astrea_graph_step(astrea_handle* h, void* state, int nsteps, void* stream) {
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
   IEngine* e = h->eng;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int trc = e->tune(state, st);
+  int trc = e->prepare(state, st);
   if (trc) return trc;
   if (!e->graph || e->graph_state != state) {
     if (e->graph) {
@@ -719,7 +810,7 @@ int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* d
 int astrea_space(astrea_handle* h, const void* state, int order, void* flux_ax0, void* flux_ax1, double* eigmax,
                  void* stream) {
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
-  int trc = h->eng->tune(state, static_cast<cudaStream_t>(stream));
+  int trc = h->eng->prepare(state, static_cast<cudaStream_t>(stream));
   if (trc) return trc;
   return h->eng->space(state, order & 1, flux_ax0, flux_ax1, eigmax, static_cast<cudaStream_t>(stream));
 }
@@ -728,7 +819,7 @@ int astrea_time(astrea_handle* h, void* state, double dt, int order, void* strea
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
   IEngine* e = h->eng;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int trc = e->tune(state, st);
+  int trc = e->prepare(state, st);
   if (trc) return trc;
   Clock c;
   std::memset(&c, 0, sizeof(c));

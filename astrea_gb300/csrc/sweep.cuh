@@ -22,6 +22,7 @@
 
 #include "physics.cuh"
 #include "recon.cuh"
+#include "tma.cuh"
 
 namespace astrea {
 
@@ -50,6 +51,7 @@ template <typename T> struct SweepArgs {
   int flatten;        // PPM: Colella (1990) flattening of the face values
   int viscosity;      // PPM: McCorquodale & Colella (2011) artificial viscosity added to the fluxes
   T av_alpha, av_beta;
+  const CUtensorMap* tmaps;  // optional (2D): TMA maps of q, indexed [axis][tile]; nullptr: plain loads
 };
 
 // plane index of primitive variable v in model M (-1 if M does not store it)
@@ -82,6 +84,22 @@ template <int SCH, int DIM, int TS, int TT> struct Geom {
   static constexpr int WT = RT;
   static constexpr int QT = DIM == 2 ? (HO ? 3 : 1) : 0;
   static constexpr int QH = TT + 2 * QT, WH = TT + 2 * WT, RH = TT + 2 * RT, FH = TT + 2 * FT;
+};
+
+// The TMA box of a tile's staged state.  Axis 1 sweeps run along the contiguous
+// axis (box x = sweep, y = rows), axis 0 sweeps across it (box x = rows, y =
+// sweep); the box's x origin is rounded down to 16 bytes and its x extent up to
+// 16 bytes, and XOFF is where the staged level starts inside the box's x.
+template <typename T, int SCH, int DIM, int AX, int TS, int TT, int NV> struct TmaBox {
+  using G = Geom<SCH, DIM, TS, TT>;
+  static constexpr int A = 16 / (int)sizeof(T);
+  static constexpr int XB = AX == 1 ? floor_to(G::Q_BEG, A) : floor_to(-G::QT, A);
+  static constexpr int BW = AX == 1 ? ceil_to(TS + G::Q_END - XB, A) : ceil_to(TT + G::QT - XB, A);
+  static constexpr int BH = AX == 1 ? G::QH : G::QW;
+  static constexpr int XOFF = AX == 1 ? G::Q_BEG - XB : -G::QT - XB;
+  static constexpr int BYTES = NV * BH * BW * (int)sizeof(T);
+  static constexpr int TILE_ID = TT == 16 ? 1 : 0;
+  static_assert(BW <= 256 && BH <= 256 && (BW * (int)sizeof(T)) % 16 == 0, "TMA box limits");
 };
 
 template <int SCH, int DIM, int TS, int TT, int NV> struct Smem {
@@ -167,7 +185,7 @@ template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, un
 // One tile: cells [s0, s0+TS) along the sweep and rows [t0, t0+TT) across it.
 // Called by the single-grid kernel (one tile per CTA) and by the batched
 // persistent kernel (a work list of tiles of many grids).
-template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, bool CL, int NT>
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, bool CL, int NT, bool TMA = false>
 __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int s0, const int t0,
                                                 unsigned char* __restrict__ smem_raw) {
   using M = Model<MID>;
@@ -205,7 +223,50 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   };
 
   // ---- level q: conservative state with halos (input boundary map), and its point primitives
-  {
+  if constexpr (TMA) {
+    // one thread issues the bulk copy of the whole box into the (still unused) R region
+    using B = TmaBox<T, SCH, DIM, AX, TS, TT, NV>;
+    __shared__ unsigned long long s_bar;
+    T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_R) + 127) & ~uintptr_t(127));
+    if (tid == 0) {
+      mbar_init(&s_bar, 1);
+      mbar_fence_init();
+      mbar_arrive_expect_tx(&s_bar, (unsigned)B::BYTES);
+      const CUtensorMap* map = a.tmaps + (AX * 2 + B::TILE_ID);
+      if (AX == 1) tma_load_3d(stage, map, s0 + B::XB, t0 - G::QT, 0, &s_bar);
+      else tma_load_3d(stage, map, t0 + B::XB, s0 + G::Q_BEG, 0, &s_bar);
+    }
+    __syncthreads();  // the barrier is initialised before anyone waits on it
+    constexpr int kWaitLimit = 1 << 16;
+    const bool landed = mbar_wait_bounded(&s_bar, 0, kWaitLimit);
+    if (!__syncthreads_and(landed)) {
+      // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
+      if (tid == 0) {
+        atomicOr(&a.clock->status, 2);
+        mbar_wait_bounded(&s_bar, 0, kWaitLimit);
+      }
+      return;
+    }
+    constexpr int W = G::QW, H = G::QH;
+    for (int e = tid; e < W * H; e += nth) {
+      int row, col;
+      if (DIM == 2 && AX == 0) { row = e % H; col = e / H; } else { col = e % W; row = e / W; }
+      T q[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) q[i] = T(0);
+#pragma unroll
+      for (int s = 0; s < NV; ++s)
+        q[M::var(s)] = AX == 1 ? stage[(s * B::BH + row) * B::BW + col + B::XOFF]
+                               : stage[(s * B::BH + col) * B::BW + row + B::XOFF];
+      const int li = row * W + col;
+      store_sm<M>(s_q, H * W, li, q);
+      if constexpr (G::HO) {
+        T w[8];
+        c2p<M>(q, w, gm1);
+        store_sm<M>(s_qw, H * W, li, w);
+      }
+    }
+  } else {
     constexpr int W = G::QW, H = G::QH;
     for (int e = tid; e < W * H; e += nth) {
       int row, col;
@@ -638,13 +699,31 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 }
 
 // Clamping is only needed on outflow grids, for tiles whose widest level
-// (the staged state) reaches past the grid edge.
-template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT = (DIM == 1 ? 64 : 256)>
+// (the staged state) reaches past the grid edge.  With TMA (single-grid 2D
+// kernels), tiles whose whole TMA box lies inside the grid are staged by the
+// bulk copy; the others load per thread as without it.
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT = (DIM == 1 ? 64 : 256),
+          bool TMA_OK = false>
 __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, const int t0,
                                            unsigned char* __restrict__ smem_raw) {
   using G = Geom<SCH, DIM, TS, TT>;
+  using S = Smem<SCH, DIM, TS, TT, Model<MID>::NV>;
   const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
   const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
+  if constexpr (TMA_OK && DIM == 2) {
+    using B = TmaBox<T, SCH, DIM, AX, TS, TT, Model<MID>::NV>;
+    if constexpr ((size_t)S::n_R * sizeof(T) >= (size_t)B::BYTES + 128) {
+      const bool box_in = a.tmaps != nullptr &&
+                          (AX == 1 ? (s0 + B::XB >= 0 && s0 + B::XB + B::BW <= a.n1 && t0 - G::QT >= 0 &&
+                                      t0 - G::QT + B::BH <= a.n0)
+                                   : (t0 + B::XB >= 0 && t0 + B::XB + B::BW <= a.n1 && s0 + G::Q_BEG >= 0 &&
+                                      s0 + G::Q_BEG + B::BH <= a.n0));
+      if (box_in) {
+        sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, true>(a, s0, t0, smem_raw);
+        return;
+      }
+    }
+  }
   const bool inside = s0 + G::Q_BEG >= 0 && s0 + TS + G::Q_END <= Ns &&
                       (DIM == 1 || (t0 - G::QT >= 0 && t0 + TT + G::QT <= Nt));
   if (a.bc == EDGE && !inside) sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, true, NT>(a, s0, t0, smem_raw);
@@ -660,7 +739,7 @@ template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT
 __global__ void __launch_bounds__(NT, (SweepOcc<T, MID, NT>::value)) sweep_kernel(const SweepArgs<T> a) {
   if (a.clock->done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT, NT>(a, blockIdx.x * TS, blockIdx.y * TT, smem_raw);
+  sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT, NT, true>(a, blockIdx.x * TS, blockIdx.y * TT, smem_raw);
 }
 
 }  // namespace astrea

@@ -1,0 +1,67 @@
+// Tensor-memory-accelerator (TMA) staging of a sweep tile: one elected thread
+// issues a 3D bulk tensor copy of the tile's conservative state (all variable
+// planes, halos included) into shared memory, completing on an mbarrier.
+//
+// Every wait is bounded: a copy that does not land within the limit sets bit 1
+// of the grid clock's status, and the CTA stops after waiting (bounded again)
+// for the copy it issued.
+#pragma once
+#include <cuda.h>
+
+#include "fv_common.cuh"
+
+namespace astrea {
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// make the initialised barrier visible to the asynchronous (TMA) proxy
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// bounded wait for phase ``parity`` of the barrier; false if the limit ran out
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity, int limit) {
+  for (int i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// 3D tiled bulk copy global -> shared (box origin x innermost); x * element size must be a multiple of 16
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// floor / ceil of x to a multiple of a (a > 0), valid for negative x
+constexpr int floor_to(int x, int a) { return x >= 0 ? (x / a) * a : -((-x + a - 1) / a) * a; }
+constexpr int ceil_to(int x, int a) { return ((x + a - 1) / a) * a; }
+
+}  // namespace astrea

@@ -45,9 +45,13 @@ sys.path.insert(0, ROOT)
 SEED = 20261203
 METRIC = "cell-updates/s FP32-batched vs FP64 plain (L1<=1e-5); serve p50/p99 ms"
 WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc) with flattening and artificial viscosity + HLLC + SSPRK3, CFL 0.8"
-# DRAM bytes (read + write) of one stage-0 sweep launch of the headline FP32
-# workload, measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum)
-SWEEP_DRAM_BYTES = 103.7e6
+# Mean DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per sweep launch
+# over the SSPRK3 steps of the headline FP32 workload at 2048^2, from one ncu
+# launch list (profiles/sweep_kernel_f32_ppm_hllc_2d.md); scaled by cells for
+# other sizes.  Below the algorithmic bytes because the L2 keeps part of each
+# stage's output for the next launch.
+SWEEP_DRAM_BYTES = 146.6e6
+SWEEP_DRAM_CELLS = 2048 * 2048
 
 
 def shear_layer(n, seed=SEED):
@@ -486,7 +490,7 @@ def main():
     peak, peak_kind = measured_peaks()
     step_alg = cells * 8 * C * sz  # 8 state passes per SSPRK3 step: the minimum traffic
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": SWEEP_DRAM_BYTES * (alg_per_launch / (2 * cells * C * sz)),
+                "traffic": SWEEP_DRAM_BYTES * cells / SWEEP_DRAM_CELLS,
                 "kernel": "sweep_kernel (every sweep launch of the timed steps)", "peak_source": peak_kind,
                 "alg_bytes_per_launch": alg_per_launch, "step_frac": step_alg * (value / ws) / cells / 1e9 / peak,
                 "note": "ALU/issue-bound stencil: thousands of FP32 ops per cell-update against 128 B"}

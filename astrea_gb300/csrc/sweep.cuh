@@ -292,10 +292,13 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   __syncthreads();
 
   // ---- level wS: cell-averaged primitives
+  // (items laid out with the staged level's row pitch, so that a warp's loads
+  // stay in consecutive banks across a row change; the two extra columns idle)
   {
     constexpr int W = G::WW, H = G::WH, QW = G::QW, QH = G::QH;
-    for (int e = tid; e < W * H; e += nth) {
-      const int row = e / W, col = e % W;
+    for (int e = tid; e < QW * H; e += nth) {
+      const int row = e / QW, col = e % QW;
+      if (col >= W) continue;
       const int vs = s0 + G::W_BEG + col, vt = t0 - G::WT + row;
       const int rs = rs_(vs), rt = DIM == 2 ? rt_(vt) : 0;
       const int qc = rs - (s0 + G::Q_BEG), qr = rt - (t0 - G::QT);
@@ -431,8 +434,9 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     constexpr int K = PpmStrip<G::RW, DIM>::K, NS = G::RW / K;
     constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
     for (int e = tid; e < NS * H * NV; e += nth) {
-      const int s = e / (NS * H), rem = e % (NS * H);
-      const int row = rem / NS, col0 = (rem % NS) * K;
+      // strip-major order: a warp's threads sit on consecutive rows (fewer bank conflicts)
+      const int strip = e / (NV * H), rem = e % (NV * H);
+      const int s = rem / H, row = rem % H, col0 = strip * K;
       const int vs0 = s0 + G::R_BEG + col0, vt = t0 - G::RT + row;
       const T* wrow = s_w + (s * WH + row + (G::WT - G::RT)) * WW - (s0 + G::W_BEG);
       T* rl = s_R + ((0 * NV + s) * H + row) * W + col0;
@@ -591,8 +595,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     T* s_fp = s_fa + 2 * NV * H * W;
     T* s_fm = s_fa + 3 * NV * H * W;
     T* s_Fa = s_fa + 4 * NV * H * W;
-    for (int e = tid; e < W * H; e += nth) {
-      const int row = e / W, col = e % W;
+    // items with the R level's row pitch (conflict-free loads across a row change)
+    for (int e = tid; e < G::RW * H; e += nth) {
+      const int row = e / G::RW, col = e % G::RW;
+      if (col >= W) continue;
       const int vk = s0 + col, vt = t0 - G::FT + row;
       if (vk > Ns) continue;
       const int rt = rt_(vt);

@@ -135,11 +135,15 @@ static EncodeTiledFn encode_tiled() {
 // TMA box (x, y) of scheme ``scheme`` for (axis, tile): the kernels' TmaBox
 template <typename T, int SCH> static void box_of(int ax, int tile, cuuint32_t* bw, cuuint32_t* bh) {
   if (ax == 0) {
-    if (tile == 0) { *bw = TmaBox<T, SCH, 2, 0, 32, 8, 1>::BW; *bh = TmaBox<T, SCH, 2, 0, 32, 8, 1>::BH; }
-    else { *bw = TmaBox<T, SCH, 2, 0, 32, 16, 1>::BW; *bh = TmaBox<T, SCH, 2, 0, 32, 16, 1>::BH; }
+    using B0 = TmaBox<T, SCH, 2, 0, Tile2<0>::TS, Tile2<0>::TT, 1>;
+    using B1 = TmaBox<T, SCH, 2, 0, Tile2<1>::TS, Tile2<1>::TT, 1>;
+    if (tile == 0) { *bw = B0::BW; *bh = B0::BH; }
+    else { *bw = B1::BW; *bh = B1::BH; }
   } else {
-    if (tile == 0) { *bw = TmaBox<T, SCH, 2, 1, 32, 8, 1>::BW; *bh = TmaBox<T, SCH, 2, 1, 32, 8, 1>::BH; }
-    else { *bw = TmaBox<T, SCH, 2, 1, 32, 16, 1>::BW; *bh = TmaBox<T, SCH, 2, 1, 32, 16, 1>::BH; }
+    using B0 = TmaBox<T, SCH, 2, 1, Tile2<0>::TS, Tile2<0>::TT, 1>;
+    using B1 = TmaBox<T, SCH, 2, 1, Tile2<1>::TS, Tile2<1>::TT, 1>;
+    if (tile == 0) { *bw = B0::BW; *bh = B0::BH; }
+    else { *bw = B1::BW; *bh = B1::BH; }
   }
 }
 template <typename T> static void box_for(int scheme, int ax, int tile, cuuint32_t* bw, cuuint32_t* bh) {

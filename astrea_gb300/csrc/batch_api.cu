@@ -20,7 +20,7 @@ using namespace astrea;
 namespace astrea {
 ASTREA_EXTERN_BATCH(float)
 ASTREA_EXTERN_BATCH(double)
-ASTREA_EXTERN_BATCH_T16
+ASTREA_EXTERN_BATCH_T2
 }  // namespace astrea
 
 template <typename T> static BatchFn<T> batched_for(int model, int dim, int ax, int v) {

@@ -1,4 +1,4 @@
-// Batched sweep kernels: float, 2D, model 4 axis 1, 32 x 16 tiles.
+// Batched sweep kernels: float, 2D, model 4 axis 1, 32 x 15 tiles.
 #include "batch_launch.cuh"
 namespace astrea {
 ASTREA_BATCH_INST(float, 4, 2, 1, 1)

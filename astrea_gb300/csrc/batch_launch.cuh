@@ -8,13 +8,13 @@
 namespace astrea {
 
 // Tiles: 1D 32 cells x 64 threads.  2D candidates, picked per batch by its
-// autotuner: 32 (sweep) x 8 (rows) x 256 threads, and 32 x 16 x 512 threads
+// autotuner: 32 (sweep) x 8 (rows) x 256 threads, and 32 x 15 x 512 threads
 // (FP32 2D Euler only, whose shared memory and registers allow it).
 constexpr int BTS1 = 32, BNT1 = 64;
 constexpr int NBTILES2 = 2;
 template <int V> struct BTile2;
 template <> struct BTile2<0> { static constexpr int TS = 32, TT = 8, NT = 256; };
-template <> struct BTile2<1> { static constexpr int TS = 32, TT = 16, NT = 512; };
+template <> struct BTile2<1> { static constexpr int TS = 32, TT = 15, NT = 512; };
 
 template <typename T> using BatchFn = cudaError_t (*)(const BatchArgs<T>&, int nctas, cudaStream_t);
 
@@ -101,7 +101,7 @@ template <typename T, int DIM> int get_occupancy(int model, int ax, int v) {
   ASTREA_BATCH_EXTERN(T, 8, 2, 1, 0)
 
 // the second 2D tile exists for FP32 2D Euler only
-#define ASTREA_EXTERN_BATCH_T16         \
+#define ASTREA_EXTERN_BATCH_T2         \
   ASTREA_BATCH_EXTERN(float, 4, 2, 0, 1) \
   ASTREA_BATCH_EXTERN(float, 4, 2, 1, 1)
 

@@ -90,16 +90,27 @@ template <int SCH, int DIM, int TS, int TT> struct Geom {
 // axis (box x = sweep, y = rows), axis 0 sweeps across it (box x = rows, y =
 // sweep); the box's x origin is rounded down to 16 bytes and its x extent up to
 // 16 bytes, and XOFF is where the staged level starts inside the box's x.
+// When TT is not a multiple of 16 bytes' worth of elements (axis 0 sweeps), the
+// x origin of a tile's box is rounded down per tile (DYN) and the box is wide
+// enough for every remainder.
 template <typename T, int SCH, int DIM, int AX, int TS, int TT, int NV> struct TmaBox {
   using G = Geom<SCH, DIM, TS, TT>;
   static constexpr int A = 16 / (int)sizeof(T);
+  static constexpr bool DYN = AX == 0 && TT % A != 0;
   static constexpr int XB = AX == 1 ? floor_to(G::Q_BEG, A) : floor_to(-G::QT, A);
-  static constexpr int BW = AX == 1 ? ceil_to(TS + G::Q_END - XB, A) : ceil_to(TT + G::QT - XB, A);
+  static constexpr int BW = AX == 1 ? ceil_to(TS + G::Q_END - XB, A)
+                                    : (DYN ? ceil_to(G::QH + A - 1, A) : ceil_to(TT + G::QT - XB, A));
   static constexpr int BH = AX == 1 ? G::QH : G::QW;
   static constexpr int XOFF = AX == 1 ? G::Q_BEG - XB : -G::QT - XB;
   static constexpr int BYTES = NV * BH * BW * (int)sizeof(T);
-  static constexpr int TILE_ID = TT == 16 ? 1 : 0;
+  static constexpr int TILE_ID = TT == 8 ? 0 : 1;
   static_assert(BW <= 256 && BH <= 256 && (BW * (int)sizeof(T)) % 16 == 0, "TMA box limits");
+  // x origin of the box and the staged level's first column inside it, for the tile at (s0, t0)
+  __host__ __device__ static int x0(int s0, int t0) {
+    if (AX == 1) return s0 + XB;
+    return DYN ? ((t0 - G::QT) / A) * A : t0 + XB;  // t0 - QT >= 0 whenever the box is used
+  }
+  __host__ __device__ static int xoff(int t0) { return DYN ? (t0 - G::QT) - x0(0, t0) : XOFF; }
 };
 
 template <int SCH, int DIM, int TS, int TT, int NV> struct Smem {
@@ -233,8 +244,8 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       mbar_fence_init();
       mbar_arrive_expect_tx(&s_bar, (unsigned)B::BYTES);
       const CUtensorMap* map = a.tmaps + (AX * 2 + B::TILE_ID);
-      if (AX == 1) tma_load_3d(stage, map, s0 + B::XB, t0 - G::QT, 0, &s_bar);
-      else tma_load_3d(stage, map, t0 + B::XB, s0 + G::Q_BEG, 0, &s_bar);
+      if (AX == 1) tma_load_3d(stage, map, B::x0(s0, t0), t0 - G::QT, 0, &s_bar);
+      else tma_load_3d(stage, map, B::x0(s0, t0), s0 + G::Q_BEG, 0, &s_bar);
     }
     __syncthreads();  // the barrier is initialised before anyone waits on it
     constexpr int kWaitLimit = 1 << 16;
@@ -248,6 +259,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       return;
     }
     constexpr int W = G::QW, H = G::QH;
+    const int xo = B::xoff(t0);
     for (int e = tid; e < W * H; e += nth) {
       int row, col;
       if (DIM == 2 && AX == 0) { row = e % H; col = e / H; } else { col = e % W; row = e / W; }
@@ -256,8 +268,8 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       for (int i = 0; i < 8; ++i) q[i] = T(0);
 #pragma unroll
       for (int s = 0; s < NV; ++s)
-        q[M::var(s)] = AX == 1 ? stage[(s * B::BH + row) * B::BW + col + B::XOFF]
-                               : stage[(s * B::BH + col) * B::BW + row + B::XOFF];
+        q[M::var(s)] = AX == 1 ? stage[(s * B::BH + row) * B::BW + col + xo]
+                               : stage[(s * B::BH + col) * B::BW + row + xo];
       const int li = row * W + col;
       store_sm<M>(s_q, H * W, li, q);
       if constexpr (G::HO) {
@@ -722,7 +734,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
       const bool box_in = a.tmaps != nullptr &&
                           (AX == 1 ? (s0 + B::XB >= 0 && s0 + B::XB + B::BW <= a.n1 && t0 - G::QT >= 0 &&
                                       t0 - G::QT + B::BH <= a.n0)
-                                   : (t0 + B::XB >= 0 && t0 + B::XB + B::BW <= a.n1 && s0 + G::Q_BEG >= 0 &&
+                                   : (t0 - G::QT >= 0 && B::x0(s0, t0) + B::BW <= a.n1 && s0 + G::Q_BEG >= 0 &&
                                       s0 + G::Q_BEG + B::BH <= a.n0));
       if (box_in) {
         sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, true>(a, s0, t0, smem_raw);

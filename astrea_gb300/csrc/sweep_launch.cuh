@@ -9,14 +9,15 @@ namespace astrea {
 template <typename T> using SweepFn = cudaError_t (*)(const SweepArgs<T>&, cudaStream_t);
 
 // Tiles: 1D 32 cells x 64 threads.  2D candidates, picked per grid by the
-// engine's autotuner: 32 (sweep) x 8 (rows) x 256 threads, and 32 x 16 x 512
-// threads (fewer transverse halo rows per cell, same threads per SM; FP32
-// Euler tiles only, whose shared memory and 64 registers allow it).
+// engine's autotuner: 32 (sweep) x 8 (rows) x 256 threads, and 32 x 15 x 512
+// threads (fewer transverse halo rows per cell, same threads per SM, and the
+// 15 x 33 interfaces of the second face level fit one pass of 512 threads;
+// FP32 Euler tiles only, whose shared memory and 64 registers allow it).
 constexpr int TS1 = 32, NT1 = 64;
 constexpr int NTILES2 = 2;
 template <int I> struct Tile2;
 template <> struct Tile2<0> { static constexpr int TS = 32, TT = 8, NT = 256; };
-template <> struct Tile2<1> { static constexpr int TS = 32, TT = 16, NT = 512; };
+template <> struct Tile2<1> { static constexpr int TS = 32, TT = 15, NT = 512; };
 
 template <typename T, int MID, int SCH, int DIM, int TS, int TT> constexpr size_t sweep_smem_bytes() {
   return sizeof(T) * (size_t)Smem<SCH, DIM, TS, TT, Model<MID>::NV>::total;

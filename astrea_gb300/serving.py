@@ -146,14 +146,16 @@ class ServeStats:
     latencies_ms: list = field(default_factory=list)
     cell_updates: float = 0.0
     wall_s: float = 0.0
-    failed: int = 0
+    failed: int = 0   # requests retired with a non-zero status (non-finite state, or stalled)
+    stalled: int = 0  # of those, retired for exceeding the step limit
     max_active: int = 0
+    unfinished: list = field(default_factory=list)  # requests cut off by the wall-clock cap (diagnostics)
 
     def summary(self):
         lat = np.array(self.latencies_ms) if self.latencies_ms else np.array([math.nan])
         return {"requests": len(self.latencies_ms), "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "cell_updates_per_s": self.cell_updates / max(self.wall_s, 1e-9),
-                "wall_s": self.wall_s, "non_finite": self.failed, "max_active": self.max_active}
+                "wall_s": self.wall_s, "failed": self.failed, "stalled": self.stalled, "max_active": self.max_active}
 
 
 class Server:
@@ -162,8 +164,11 @@ class Server:
     CLASSES = ((1, 3), (1, 8), (2, 4), (2, 8))
 
     def __init__(self, hbm_budget_bytes=150e9, precision=32, max_slots=256, shares=None, keep_results=False,
-                 steps_per_poll=4, device=None):
+                 steps_per_poll=4, device=None, max_steps=None):
         self.precision = precision
+        # a request whose time step collapsed (near-vacuum states with finite speeds) would never reach its
+        # end time; past ``max_steps`` steps it is retired with status bit 2
+        self.max_steps = max_steps
         esize = 4 if precision == 32 else 8
         shares = shares or {(1, 3): .1, (1, 8): .1, (2, 4): .5, (2, 8): .3}
         self.device = torch.device(device or "cuda")
@@ -239,14 +244,17 @@ class Server:
                     clk = self.batches[cls].clocks()
                 now = time.perf_counter() - t0
                 for slot in list(self.active[cls].keys()):
-                    if not clk["done"][slot]:
+                    over = self.max_steps is not None and clk["steps"][slot] > self.max_steps
+                    if not clk["done"][slot] and not over:
                         continue
                     r, off, size = self.active[cls].pop(slot)
                     r.finished = now
                     r.steps = int(clk["steps"][slot])
-                    r.status = int(clk["status"][slot])
+                    r.status = int(clk["status"][slot]) | (4 if over and not clk["done"][slot] else 0)
                     if r.status:
                         stats.failed += 1
+                    if r.status & 4:
+                        stats.stalled += 1
                     stats.cell_updates += r.cells * r.steps
                     stats.latencies_ms.append(1e3 * (r.finished - r.arrival))
                     if self.keep_results:
@@ -257,4 +265,17 @@ class Server:
                     self.free_slots[cls].append(slot)
         torch.cuda.synchronize(self.device)
         stats.wall_s = time.perf_counter() - t0
+        # requests still running when the wall-clock cap ends the loop give their slots and memory back
+        for cls in self.classes:
+            clk = self.batches[cls].clocks() if self.active[cls] else None
+            for slot, (r, off, size) in list(self.active[cls].items()):
+                stats.unfinished.append({"rid": r.rid, "class": cls, "n": r.n, "scheme": r.scheme, "solver": r.solver,
+                                         "t_end": r.t_end, "t": float(clk["t"][slot]), "dt": float(clk["dt"][slot]),
+                                         "steps": int(clk["steps"][slot]), "status": int(clk["status"][slot])})
+                self.batches[cls].release(slot)
+                self.arenas[cls].release(off, size)
+                self.free_slots[cls].append(slot)
+            self.active[cls] = {}
+            for r in pending[cls]:
+                stats.unfinished.append({"rid": r.rid, "class": cls, "n": r.n, "pending": True})
         return stats

@@ -407,17 +407,25 @@ def sod_oracle(n=4096):
     return q, t, steps, wall
 
 
-def serving_leg(count, rate, seed=SEED):
+def serving_leg(count, rates, seed=SEED, max_wall_s=30.0):
+    """Seeded request streams at each arrival rate: p50/p99 latency and aggregate cell-updates/s."""
     from astrea_gb300.serving import Server, make_requests
-    reqs = make_requests(count, rate, seed=seed, n1d=(64, 16384), n2d=(32, 512))
-    srv = Server(hbm_budget_bytes=150e9, precision=32, max_slots=256, steps_per_poll=8)
-    stats = srv.serve(reqs, max_wall_s=60.0)
-    out = stats.summary()
-    out["unfinished"] = count - out["requests"]
-    out.update({"rate_per_s": rate, "mix": "40% 1D N log-U[64,16384], 60% 2D side log-U[32,512] (full mix / 4 per "
-                                         "axis), Euler|MHD 50/50, {PLM,PPM,WENO5}x{LLF,HLLC|HLLD}, t_end U[.05,.3]",
-                "hbm_budget_gb": 150})
-    return out
+    # the largest request of this mix needs ~2e4 steps; a request past 5e4 has a collapsed time step
+    srv = Server(hbm_budget_bytes=150e9, precision=32, max_slots=256, steps_per_poll=8, max_steps=50000)
+    sweep = []
+    for i, rate in enumerate(rates):
+        reqs = make_requests(count, rate, seed=seed + i, n1d=(64, 16384), n2d=(32, 512))
+        stats = srv.serve(reqs, max_wall_s=max_wall_s)
+        out = stats.summary()
+        out["unfinished"] = count - out["requests"]
+        out["rate_per_s"] = rate
+        sweep.append(out)
+    head = dict(sweep[0])
+    head.update({"rates": sweep, "requests_per_rate": count,
+                 "mix": "40% 1D N log-U[64,16384], 60% 2D side log-U[32,512] (the full mix / 4 per axis), "
+                        "Euler|MHD 50/50, {PLM,PPM,WENO5}x{LLF,HLLC|HLLD}, t_end U[.05,.3], FP32",
+                 "hbm_budget_gb": 150})
+    return head
 
 
 def main():
@@ -431,7 +439,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=120)
-    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-rates", default="50,500,2000", help="arrival rates (requests/s) of the serving sweep")
     ap.add_argument("--mhd-n", type=int, default=1024)
     ap.add_argument("--mhd-steps", type=int, default=20)
     ap.add_argument("--sod-n", type=int, default=4096)
@@ -552,7 +560,7 @@ def main():
     if not args.no_extras:
         batched = batched_leg(args.batch_steps, 2)
         torch.cuda.empty_cache()
-        serving = serving_leg(args.serve_requests, args.serve_rate)
+        serving = serving_leg(args.serve_requests, [float(r) for r in args.serve_rates.split(",")])
         torch.cuda.empty_cache()
         mhd = mhd_leg(args.mhd_n, args.mhd_steps)
         torch.cuda.empty_cache()

@@ -384,15 +384,18 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
           const int y = rs_(s0 + CB_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
           auto P = [&](int x) -> T { return wv(PP, x, rt); };
           const T dp1 = P(rs_(y + 1)) - P(rs_(y - 1));
-          const T dp2 = P(rs_(y + 2)) - P(rs_(y - 2));
-          const T z = dvd(abs_(dp1), abs_(dp2));
-          T cb = T(1) - dvd(z - T(.75), T(DZ));
-          if (z > T(.85)) cb = T(0);
-          if (z < T(.75)) cb = T(1);
-          // only strong, compressive pressure jumps are flattened (Colella & Woodward 1984, A.1)
+          // only strong, compressive pressure jumps are flattened (Colella & Woodward 1984, A.1);
+          // elsewhere chi_bar = 1 and z is not needed
           const bool not_compressive = (wv(PN, rs_(y - 1), rt) - wv(PN, rs_(y + 1), rt)) <= T(0);
           const bool weak = dvd(abs_(dp1), npmin(P(rs_(y + 1)), P(rs_(y - 1)))) <= T(.33);
-          if (not_compressive || weak) cb = T(1);
+          T cb = T(1);
+          if (!(not_compressive || weak)) {
+            const T dp2 = P(rs_(y + 2)) - P(rs_(y - 2));
+            const T z = dvd(abs_(dp1), abs_(dp2));
+            cb = T(1) - dvd(z - T(.75), T(DZ));
+            if (z > T(.85)) cb = T(0);
+            if (z < T(.75)) cb = T(1);
+          }
           s_cb[row * CW + col] = cb;
         }
         __syncthreads();
@@ -423,11 +426,14 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
             const T dvt_xp = wv(PT, xp, rp) - wv(PT, xp, rm);
             lam = lam + T(.25) * (dvt_xp + dvt_x);
           }
-          const T cs_x = sqrt_(dvd(gamma * wv(PP, x, rt), wv(PR, x, rt)));
-          const T cs_xp = sqrt_(dvd(gamma * wv(PP, xp, rt), wv(PR, xp, rt)));
-          const T cmin = npmin(cs_x, cs_xp);
-          T nu = npmin(T(1), dvd(lam * lam, a.av_beta * (cmin * cmin))) * lam;
-          if (lam >= T(0)) nu = T(0);
+          // only compressive faces are viscous; the coefficient is formed only there
+          T nu = T(0);
+          if (!(lam >= T(0))) {
+            const T cs_x = sqrt_(dvd(gamma * wv(PP, x, rt), wv(PR, x, rt)));
+            const T cs_xp = sqrt_(dvd(gamma * wv(PP, xp, rt), wv(PR, xp, rt)));
+            const T cmin = npmin(cs_x, cs_xp);
+            nu = npmin(T(1), dvd(lam * lam, a.av_beta * (cmin * cmin))) * lam;
+          }
           const T* qrow = s_q + (rt - (t0 - G::QT)) * G::QW - (s0 + G::Q_BEG);
 #pragma unroll
           for (int v = 0; v < NV; ++v) {

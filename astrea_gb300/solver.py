@@ -162,6 +162,13 @@ class Solver:
                                               ctypes.c_void_p(self.state.data_ptr()), _stream()))
         torch.cuda.current_stream().synchronize()
 
+    def initialise_planes(self, prim):
+        """Point primitives already in the state layout (nv, n0, n1) on the device -> cell-averaged conservatives."""
+        prim = prim.to(dtype=self.cfg.dtype).contiguous()
+        _lib.check(self.lib.astrea_initialise(self.handle, ctypes.c_void_p(prim.data_ptr()),
+                                              ctypes.c_void_p(self.state.data_ptr()), _stream()))
+        torch.cuda.current_stream().synchronize()
+
     def conservative(self):
         """The state as a reference-layout (n0[, n1], 8) tensor."""
         return from_planes(self.state, self.cfg.model, self.cfg.dim)

@@ -188,6 +188,39 @@ int astrea_reduce_conserved_static(const void* state, int precision, long long c
                                    void* stream);
 
 /* ------------------------------------------------------------------------
+ * Initial conditions on the device (functions/constructor.py:11-103).
+ * Point primitives of a test problem, evaluated per cell from the values the
+ * reference's test table puts into ``sim_variables`` (initial_left/right,
+ * start/end/shock positions, misc parameters), so that nothing grid-sized is
+ * uploaded.  ``kind`` follows constructor.initialise's dispatch on the config
+ * name; astrea_gb300/initial.py maps names and ``sim_variables`` onto this. */
+enum astrea_ic_kind {
+  ASTREA_IC_SPLIT = 0,     /* one jump: 2D x < shock, 1D x <= shock (1D |x| <= shock with abs_mask) */
+  ASTREA_IC_RADIAL = 1,    /* 2D sedov / blast / rotor: disc of radius shock - centre */
+  ASTREA_IC_GAUSS = 2,     /* gaussian density bump (1D or 2D) */
+  ASTREA_IC_KHI = 3,       /* 2D Kelvin-Helmholtz: jump across y, sine v_y perturbation */
+  ASTREA_IC_VORTEX = 4,    /* 2D isentropic vortex */
+  ASTREA_IC_QUADRANT = 5,  /* 2D Lax-Liu four quadrants */
+  ASTREA_IC_OT = 6,        /* 2D Orszag-Tang */
+  ASTREA_IC_SHU = 7,       /* 1D Shu-Osher: sine density right of the jump */
+  ASTREA_IC_SINE = 8,      /* 1D sine density */
+  ASTREA_IC_LINEAR = 9,    /* 1D linear sound wave */
+  ASTREA_IC_LINEAR_MHD = 10 /* 1D linear Alfven wave */
+};
+typedef struct astrea_ic {
+  int kind, abs_mask;
+  int dim, n;              /* n cells per axis */
+  double start, end, shock;
+  double left[8], right[8], bottom_left[8], bottom_right[8];
+  double ampl, freq, y_offset, fwhm, peak_pos, perturb_ampl, vortex_str, omega;
+  double gamma;
+} astrea_ic;
+/* Write the point primitives of ``ic`` into ``prim_out`` (device, the model's
+ * planes, float or double by ``precision``); astrea_initialise then forms the
+ * cell averages.  Asynchronous on ``stream``. */
+int astrea_point_state(const astrea_ic* ic, int precision, int model, void* prim_out, void* stream);
+
+/* ------------------------------------------------------------------------
  * Batched engine: many independent grids of uneven sizes in one state arena.
  * The reference runs one grid per process (astrea.py:155-190 loops over
  * resolutions one after another); a batch advances every occupied slot per

@@ -103,6 +103,19 @@ class SlotBatch:
         _lib.check(self.lib.astrea_batch_initialise(self.handle, int(slot), ctypes.c_void_p(self.prim_arena.data_ptr()),
                                                     ctypes.c_void_p(self.arena.data_ptr()), _stream()))
 
+    def occupy_ic(self, slot, cfg, offset, ic):
+        """Like ``occupy``, with the point primitives built on the device from an ``initial.IC``."""
+        from . import initial
+        spec = spec_of(cfg)
+        _lib.check(self.lib.astrea_batch_set(self.handle, int(slot), ctypes.byref(spec), int(offset)))
+        self.slots[slot] = (cfg, int(offset))
+        lib = initial._lib_ic()
+        esize = self.prim_arena.element_size()
+        ptr = self.prim_arena.data_ptr() + int(offset) * esize
+        _lib.check(lib.astrea_point_state(ctypes.byref(ic), self.precision, self.model, ctypes.c_void_p(ptr), _stream()))
+        _lib.check(self.lib.astrea_batch_initialise(self.handle, int(slot), ctypes.c_void_p(self.prim_arena.data_ptr()),
+                                                    ctypes.c_void_p(self.arena.data_ptr()), _stream()))
+
     def release(self, slot):
         _lib.check(self.lib.astrea_batch_clear(self.handle, int(slot)))
         self.slots.pop(slot, None)

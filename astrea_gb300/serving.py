@@ -68,8 +68,8 @@ class Request:
                          boundary=self.boundary, gamma=self.gamma, dx=1.0 / self.n, cfl=self.cfl, t_end=self.t_end,
                          compat=self.compat)
 
-    def initial_state(self):
-        """Point primitives: seeded Riemann data (two states in 1D, four quadrants in 2D)."""
+    def states(self):
+        """The seeded Riemann states: two in 1D (left, right), four in 2D (quadrants in row-major order)."""
         rng = np.random.default_rng(self.seed)
 
         def state():
@@ -81,15 +81,33 @@ class Request:
                 s[5:8] = rng.uniform(-1, 1, 3)
             return s
 
+        return [state() for _ in range(2 if self.dim == 1 else 4)]
+
+    def initial_state(self):
+        """Point primitives on the host: seeded Riemann data (two states in 1D, four quadrants in 2D)."""
+        st = self.states()
         n = self.n
         if self.dim == 1:
             w = np.zeros((n, 8))
-            w[: n // 2], w[n // 2:] = state(), state()
+            w[: n // 2], w[n // 2:] = st
         else:
             w = np.zeros((n, n, 8))
             h = n // 2
-            w[:h, :h], w[:h, h:], w[h:, :h], w[h:, h:] = state(), state(), state(), state()
+            w[:h, :h], w[:h, h:], w[h:, :h], w[h:, h:] = st
         return w
+
+    def ic(self):
+        """The same data as an ``initial.IC`` for the device builder: a jump at x = 1/2 on [0, 1] (even n)."""
+        from . import initial
+        st = self.states()
+        c = initial.IC(kind=initial.SPLIT if self.dim == 1 else initial.QUADRANT, abs_mask=0, dim=self.dim, n=self.n,
+                       start=0.0, end=1.0, shock=0.5, gamma=self.gamma)
+        slots = ("left", "right") if self.dim == 1 else ("left", "bottom_left", "right", "bottom_right")
+        for name, s in zip(slots, st):
+            arr = getattr(c, name)
+            for k in range(8):
+                arr[k] = float(s[k])
+        return c
 
 
 def make_requests(count, rate, seed=20261203, n1d=(256, 65536), n2d=(128, 2048), frac_1d=0.4, frac_mhd=0.5,
@@ -197,7 +215,8 @@ class Server:
             return False
         slot = self.free_slots[cls].pop()
         with torch.cuda.stream(self.streams[cls]):
-            self.batches[cls].occupy(slot, r.config(self.precision), off, r.initial_state())
+            # the initial state is built on the device from the request's few Riemann states
+            self.batches[cls].occupy_ic(slot, r.config(self.precision), off, r.ic())
         r.admitted = now
         self.active[cls][slot] = (r, off, size)
         return True

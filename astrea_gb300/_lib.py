@@ -16,7 +16,7 @@ EXPORTS = [
     "astrea_version", "astrea_last_error", "astrea_create", "astrea_destroy", "astrea_layout", "astrea_initialise",
     "astrea_reset_clock", "astrea_step", "astrea_graph_step", "astrea_get_clock", "astrea_space", "astrea_time",
     "astrea_to_primitive", "astrea_reduce_conserved", "astrea_step_timed", "astrea_reduce_conserved_static",
-    "astrea_sweep_tile", "astrea_point_state",
+    "astrea_sweep_tile", "astrea_point_state", "astrea_total_variation", "astrea_solution_error",
 ]
 
 

@@ -180,6 +180,13 @@ class Solver:
                                                 ctypes.c_void_p(out.data_ptr()), _stream()))
         return from_planes(out, self.cfg.model, self.cfg.dim)
 
+    def primitive_planes(self):
+        """The primitive snapshot as the model's planes on the device (for astrea_gb300.diagnostics)."""
+        out = torch.empty_like(self.state)
+        _lib.check(self.lib.astrea_to_primitive(self.handle, ctypes.c_void_p(self.state.data_ptr()),
+                                                ctypes.c_void_p(out.data_ptr()), _stream()))
+        return out
+
     # -- time stepping ----------------------------------------------------------
     def reset_clock(self, t=0.0, idx=1, order=0):
         _lib.check(self.lib.astrea_reset_clock(self.handle, float(t), int(idx), int(order), _stream()))

@@ -221,6 +221,24 @@ typedef struct astrea_ic {
 int astrea_point_state(const astrea_ic* ic, int precision, int model, void* prim_out, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Diagnostics of a primitive snapshot (functions/analytic.py).  ``prim`` (and
+ * ``ref``) hold the model's primitive planes on the device (n1 = 1 in 1D).
+ * Ten quantities per result: the eight primitives (rho, v_x, v_y, v_z, P, B_x,
+ * B_y, B_z; absent ones are zero), the specific total energy E_tot = e_tot/rho
+ * and the specific internal energy E_int = P/(rho (gamma - 1)).  Sums are FP64
+ * and compensated; the partials live in a fixed device array (no allocation),
+ * so calls on one device must not overlap.  Both synchronise ``stream``. */
+/* calculate_TV (analytic.py:48-63): sum of |differences| after differencing
+ * along axis 0 and then axis 1 (in 2D the mixed difference). */
+int astrea_total_variation(const void* prim, int precision, int model, int dim, int n0, int n1, double gamma,
+                           double* tv_host, void* stream);
+/* calculate_solution_error (analytic.py:24-45) against ``ref`` (e.g. the initial
+ * state of a periodic test after whole periods): norm <= 0 gives the L1 norm,
+ * norm > 10 the maximum, otherwise the L_norm norm, each normalised by n0^dim. */
+int astrea_solution_error(const void* prim, const void* ref, int precision, int model, int dim, int n0, int n1,
+                          double gamma, double norm, double* err_host, void* stream);
+
+/* ------------------------------------------------------------------------
  * Batched engine: many independent grids of uneven sizes in one state arena.
  * The reference runs one grid per process (astrea.py:155-190 loops over
  * resolutions one after another); a batch advances every occupied slot per

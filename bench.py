@@ -177,12 +177,14 @@ def cpu_baseline(n=256, procs=1, steps=1):
 
 
 def dist_init():
+    """Ranks of a torchrun launch (one replica per GPU); NCCL, or gloo for host-only runs (ASTREA_DIST_BACKEND)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        if not dist.is_initialized():
+            dist.init_process_group(os.environ.get("ASTREA_DIST_BACKEND", "nccl"))
     return ws, rank, local
 
 
@@ -197,7 +199,8 @@ def allmax(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], device=dev, dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

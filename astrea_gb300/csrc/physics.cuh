@@ -45,13 +45,15 @@ template <typename T> __device__ __forceinline__ void zero8(T* x) {
 
 // norm(v)**2 as the reference forms it (np.linalg.norm then **2: sqrt of the
 // sequential sum, squared again).  For a single non-zero component the
-// result is exactly x*x.
+// result is exactly x*x.  The FP32 path, which is not bit-compared with the
+// reference, takes the sum of squares itself (one root and one product less).
 template <class M, typename T> __device__ __forceinline__ T nsq_vel(const T* w) {
   if constexpr (!M::VY) {
     return w[1] * w[1];
   } else {
     T s = w[1] * w[1] + w[2] * w[2];
     if constexpr (M::VZ) s = s + w[3] * w[3];
+    if constexpr (!Prec<T>::EXACT) return s;
     T r = sqrt_(s);
     return r * r;
   }
@@ -60,12 +62,16 @@ template <class M, typename T> __device__ __forceinline__ T nsq_mag(const T* w) 
   if constexpr (!M::MHD) {
     return T(0);
   } else {
-    T r = sqrt_((w[5] * w[5] + w[6] * w[6]) + w[7] * w[7]);
+    const T s = (w[5] * w[5] + w[6] * w[6]) + w[7] * w[7];
+    if constexpr (!Prec<T>::EXACT) return s;
+    T r = sqrt_(s);
     return r * r;
   }
 }
 template <typename T> __device__ __forceinline__ T nsq3(T a, T b, T c) {
-  T r = sqrt_((a * a + b * b) + c * c);
+  const T s = (a * a + b * b) + c * c;
+  if constexpr (!Prec<T>::EXACT) return s;
+  T r = sqrt_(s);
   return r * r;
 }
 template <typename T> __device__ __forceinline__ T norm3(T a, T b, T c) { return sqrt_((a * a + b * b) + c * c); }

@@ -39,7 +39,7 @@ def sources():
 
 
 def flags_for(name):
-    if name.startswith(("sweep_f32", "batch_k_f32")):
+    if name.startswith(("sweep_f32", "batch_k_f32", "cellavg_f32")):
         # FP32 path: fused multiply-add, approximate division and square root, flush-to-zero
         return ["--fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
     return ["--fmad=false"]

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/astrea_gb300.h"
+#include "cellavg.cuh"
 #include "ct.cuh"
 #include "stage.cuh"
 #include "sweep_launch.cuh"
@@ -51,7 +52,7 @@ static int stages_of(int integ) {
 
 // Event pairs around kernel launches, by kernel kind (astrea_step_timed)
 struct KTimer {
-  std::vector<cudaEvent_t> ev[3][2];
+  std::vector<cudaEvent_t> ev[4][2];
   int open_kind = -1;
   cudaError_t start(int kind, cudaStream_t st) {
     cudaEvent_t e;
@@ -169,6 +170,8 @@ template <typename T> struct Engine final : IEngine {
   T* ez = nullptr;                // 2D MHD: corner electric field
   SweepFn<T> sweep[2] = {nullptr, nullptr};
   T* reg[6] = {};                    // registers of the integrators with more live stages (rk_stage_kernel)
+  T* wsb[2] = {nullptr, nullptr};    // 2D high-order schemes: the stage input's cell averages, one per sweep order
+  CellAvgFn<T> cavg = nullptr;
   // TMA maps of every buffer a sweep reads (state, stage buffers, registers): 4 per buffer ([axis][tile])
   static constexpr int kMapSlots = 16;
   CUtensorMap* d_maps = nullptr;
@@ -178,7 +181,7 @@ template <typename T> struct Engine final : IEngine {
   bool tuned = false;
 
   ~Engine() override {
-    for (int i = 0; i < 2; ++i) { cudaFree(k[i]); cudaFree(d[i]); cudaFree(wf[i]); }
+    for (int i = 0; i < 2; ++i) { cudaFree(k[i]); cudaFree(d[i]); cudaFree(wf[i]); cudaFree(wsb[i]); }
     for (T* r : reg) cudaFree(r);
     cudaFree(d_maps);
     cudaFree(tmp);
@@ -186,6 +189,10 @@ template <typename T> struct Engine final : IEngine {
   }
 
   bool ct() const { return (cfg.flags & ASTREA_FLAG_CT) != 0; }
+  // 2D high-order sweeps stage the cell averages of a pre-pass (cell_average_kernel)
+  bool use_ws() const { return cfg.dim == 2 && cfg.scheme >= PPM; }
+  // FP64: one copy per sweep order; FP32: the axis-0 order serves both sweeps
+  static constexpr int n_ws() { return cell_average_both_orders<T>() ? 2 : 1; }
 
   long long plane() const { return cells; }
 
@@ -196,6 +203,12 @@ template <typename T> struct Engine final : IEngine {
       if (cudaMalloc(&d[i], bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "divergence buffer allocation failed");
     }
     if (cudaMalloc(&tmp, bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "scratch allocation failed");
+    if (use_ws()) {
+      for (int i = 0; i < n_ws(); ++i)
+        if (cudaMalloc(&wsb[i], bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "cell-average buffer allocation failed");
+      cavg = get_cell_average<T>(cfg.model);
+      if (!cavg) return fail(ASTREA_ERR_CONFIG, "no cell-average kernel for this model");
+    }
     if (cfg.integrator >= SSPRK53) {
       const int nreg = cfg.integrator == SSPRK53 ? 6 : (cfg.integrator == SSPRK104 ? 3 : (cfg.integrator == RK4 ? 4 : 5));
       for (int i = 0; i < nreg; ++i)
@@ -228,9 +241,13 @@ template <typename T> struct Engine final : IEngine {
     const char* tma_env = std::getenv("ASTREA_TMA");
     if (cfg.dim == 2 && ((size_t)cfg.n1 * sizeof(T)) % 16 == 0 && encode_tiled() && !(tma_env && tma_env[0] == '0')) {
       CK(cudaMalloc(&d_maps, sizeof(CUtensorMap) * 4 * kMapSlots));
-      for (int i = 0; i < 2; ++i) CK(add_map(k[i]));
-      for (T* r : reg)
-        if (r) CK(add_map(r));
+      if (use_ws()) {
+        for (int i = 0; i < n_ws(); ++i) CK(add_map(wsb[i]));
+      } else {
+        for (int i = 0; i < 2; ++i) CK(add_map(k[i]));
+        for (T* r : reg)
+          if (r) CK(add_map(r));
+      }
     }
     // set the kernels' shared-memory attribute now, outside any stream capture
     SweepArgs<T> probe{};
@@ -274,7 +291,7 @@ template <typename T> struct Engine final : IEngine {
   int prepare(const void* state, cudaStream_t st) override {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     CK(cudaStreamIsCapturing(st, &cs));
-    if (cs == cudaStreamCaptureStatusNone) CK(add_map(state));
+    if (cs == cudaStreamCaptureStatusNone && !use_ws()) CK(add_map(state));
     return tune(state, st);
   }
 
@@ -315,6 +332,8 @@ template <typename T> struct Engine final : IEngine {
       a.mode = 0;
       a.want_emax = 0;
       a.dout = d[ax];
+      int prc = prep(static_cast<const T*>(state), c, st, nullptr);
+      if (prc) return prc;
       cudaEvent_t e0, e1;
       CK(cudaEventCreate(&e0));
       CK(cudaEventCreate(&e1));
@@ -322,9 +341,9 @@ template <typename T> struct Engine final : IEngine {
       int best_t = 0;
       for (int t = 0; t < NTILES2; ++t) {
         if (!cand[ax][t]) continue;
-        CK(cand[ax][t](a, st));
+        CK(run_sweep(cand[ax][t], ax, a, st));
         CK(cudaEventRecord(e0, st));
-        for (int r = 0; r < 3; ++r) CK(cand[ax][t](a, st));
+        for (int r = 0; r < 3; ++r) CK(run_sweep(cand[ax][t], ax, a, st));
         CK(cudaEventRecord(e1, st));
         CK(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -360,8 +379,25 @@ template <typename T> struct Engine final : IEngine {
     a.viscosity = (cfg.flags & ASTREA_FLAG_VISCOSITY) ? 1 : 0;
     a.av_alpha = T(0.3);
     a.av_beta = T(0.3);
-    a.tmaps = find_map(q);
+    a.tmaps = use_ws() ? nullptr : find_map(q);
     return a;
+  }
+
+  // the cell-average pre-pass of a stage input (2D high-order schemes)
+  int prep(const T* q, Clock* c, cudaStream_t st, KTimer* tm) {
+    if (!use_ws()) return ASTREA_OK;
+    TSTART(3);
+    CK(cavg(q, wsb[0], wsb[1], cfg.n0, cfg.n1, plane(), cfg.boundary, T(cfg.gamma - 1.0), c, st));
+    TSTOP();
+    return ASTREA_OK;
+  }
+  // one sweep along ``ax``, pointed at that axis's cell averages when the scheme uses them
+  cudaError_t run_sweep(SweepFn<T> fn, int ax, SweepArgs<T> a, cudaStream_t st) const {
+    if (use_ws()) {
+      a.ws = wsb[n_ws() == 2 ? ax : 0];
+      a.tmaps = find_map(a.ws);
+    }
+    return fn(a, st);
   }
 
   // 2D MHD step: per stage both sweeps (storing face values), the corner
@@ -379,11 +415,13 @@ template <typename T> struct Engine final : IEngine {
       SweepArgs<T> a = base_args(cur, c);
       a.mode = 0;
       a.want_emax = s == 0;
+      int prc = prep(cur, c, st, tm);
+      if (prc) return prc;
       for (int ax = 0; ax < 2; ++ax) {
         a.dout = d[ax];
         a.wface_out = wf[ax];
         TSTART(0);
-        CK(sweep[ax](a, st));
+        CK(run_sweep(sweep[ax], ax, a, st));
         TSTOP();
       }
       if (s == 0 && device_dt) {
@@ -447,10 +485,12 @@ template <typename T> struct Engine final : IEngine {
       SweepArgs<T> a = base_args(rk_input(s, u), c);
       a.mode = 0;
       a.want_emax = s == 0;
+      int prc = prep(rk_input(s, u), c, st, tm);
+      if (prc) return prc;
       for (int ax = 0; ax < cfg.dim; ++ax) {
         a.dout = d[ax];
         TSTART(0);
-        CK(sweep[ax](a, st));
+        CK(run_sweep(sweep[ax], ax, a, st));
         TSTOP();
       }
       if (s == 0 && device_dt) {
@@ -498,13 +538,15 @@ template <typename T> struct Engine final : IEngine {
       a.mode = 0;
       a.want_emax = 1;
       a.dout = d[0];
+      int prc = prep(u, c, st, tm);
+      if (prc) return prc;
       TSTART(0);
-      CK(sweep[0](a, st));
+      CK(run_sweep(sweep[0], 0, a, st));
       TSTOP();
       if (cfg.dim == 2) {
         a.dout = d[1];
         TSTART(0);
-        CK(sweep[1](a, st));
+        CK(run_sweep(sweep[1], 1, a, st));
         TSTOP();
       }
       if (device_dt) {
@@ -527,22 +569,24 @@ template <typename T> struct Engine final : IEngine {
       a.stage = s;
       a.u0 = u;
       a.out = out;
+      int prc = prep(cur, c, st, tm);
+      if (prc) return prc;
       if (cfg.dim == 2) {
         a.mode = 0;
         a.dout = d[0];
         TSTART(0);
-        CK(sweep[0](a, st));
+        CK(run_sweep(sweep[0], 0, a, st));
         TSTOP();
         a.mode = 1;
         a.dother = d[0];
         a.dout = nullptr;
         TSTART(0);
-        CK(sweep[1](a, st));
+        CK(run_sweep(sweep[1], 1, a, st));
         TSTOP();
       } else {
         a.mode = 2;
         TSTART(0);
-        CK(sweep[0](a, st));
+        CK(run_sweep(sweep[0], 0, a, st));
         TSTOP();
       }
     }
@@ -564,11 +608,13 @@ template <typename T> struct Engine final : IEngine {
     a.want_emax = 1;
     a.dout = d[0];
     a.flux_out = static_cast<T*>(f0);
-    CK(sweep[0](a, st));
+    int prc = prep(static_cast<const T*>(state), c, st, nullptr);
+    if (prc) return prc;
+    CK(run_sweep(sweep[0], 0, a, st));
     if (cfg.dim == 2) {
       a.dout = d[1];
       a.flux_out = static_cast<T*>(f1);
-      CK(sweep[1](a, st));
+      CK(run_sweep(sweep[1], 1, a, st));
     }
     unsigned long long e[2];
     CK(cudaMemcpyAsync(e, &c->emax[0], sizeof(e), cudaMemcpyDeviceToHost, st));
@@ -755,7 +801,7 @@ int astrea_step_timed(astrea_handle* h, void* state, int nsteps, double* kernel_
     if (rc) return rc;
   }
   CK(cudaStreamSynchronize(st));
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 4; ++k) {
     double ms = 0.0;
     for (size_t i = 0; i < tm.ev[k][0].size(); ++i) {
       float x = 0.f;

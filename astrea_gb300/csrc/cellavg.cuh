@@ -1,0 +1,165 @@
+// Cell-averaged primitives of a 2D state: the first level of the high-order
+// sweeps (fv.high_order_convert_conservative, fv.py:126-143), computed once per
+// stage for both sweeps instead of once per sweep tile with halos.
+//
+//   wS = c2p(q - d2q/24) + d2(c2p(q))/24,   d2 = the sweep axis's second
+//   difference, then the transverse one's
+//
+// The two sweeps add the two axes' corrections in opposite orders, which round
+// differently, so the kernel writes one copy per sweep: w_ax0 for the axis-0
+// sweep (axis 0 first), w_ax1 for the axis-1 sweep (FP64; see below for FP32).  Edge cells take their
+// neighbours through the input boundary map (clamp for outflow, wrap for
+// periodic), the values the sweep tiles' own q level holds there.  The
+// arithmetic is the sweep's, operation for operation.
+#pragma once
+#include "sweep.cuh"
+
+namespace astrea {
+
+// One warp per strip of 30 columns x TY rows: its 32 lanes sit on 32
+// consecutive columns (lanes 0 and 31 are the strip's halo) and walk down the
+// rows, keeping rows i-1, i, i+1 (state and point primitives) in registers and
+// taking the axis-1 neighbours from the adjacent lanes; the next row's state is
+// loaded one row ahead.  No shared memory, no block barriers.
+constexpr int CA_W = 30, CA_NT = 256, CA_WARPS = CA_NT / 32;
+template <typename T, int MID> struct CellAvgTile {
+  static constexpr int TY = 16;  // rows per strip
+};
+
+// The FP64 kernels write both sweep orders (bit-level parity); the FP32 ones
+// write the axis-0 order only, which both FP32 sweeps read (its rounding differs
+// from the other order's in the last FP32 bit).
+template <typename T> constexpr bool cell_average_both_orders() { return Prec<T>::EXACT; }
+
+template <typename T, int MID>
+__global__ void __launch_bounds__(CA_NT) cell_average_kernel(const T* __restrict__ q, T* __restrict__ w_ax0,
+                                                             T* __restrict__ w_ax1, int n0, int n1, long long plane,
+                                                             int bc, T gm1, const Clock* clk) {
+  if (clk->done) return;
+  using M = Model<MID>;
+  constexpr int NV = M::NV, TY = CellAvgTile<T, MID>::TY;
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int i0 = (blockIdx.y * CA_WARPS + (threadIdx.x >> 5)) * TY;
+  if (i0 >= n0) return;  // whole warp
+  const int j = blockIdx.x * CA_W - 1 + lane;
+  const int gj = (j >= 0 && j < n1) ? j : bc_map(j, n1, bc);
+  const bool out_lane = lane >= 1 && lane <= CA_W && j < n1;
+  auto row_ptr = [&](int i) -> const T* {
+    const int gi = (i >= 0 && i < n0) ? i : bc_map(i, n0, bc);
+    return q + (long long)gi * n1 + gj;
+  };
+  auto expand = [&](const T* v, T* x) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = T(0);
+#pragma unroll
+    for (int s = 0; s < NV; ++s) x[M::var(s)] = v[s];
+  };
+  T qm[8], q0[8], qp[8], wm[8], w0[8], wp[8], nxt[NV];
+  {
+    const T* pm = row_ptr(i0 - 1);
+    const T* p0 = row_ptr(i0);
+    const T* p1 = row_ptr(i0 + 1);
+    T a[NV], b[NV];
+#pragma unroll
+    for (int s = 0; s < NV; ++s) { a[s] = pm[s * plane]; b[s] = p0[s * plane]; nxt[s] = p1[s * plane]; }
+    expand(a, qm);
+    expand(b, q0);
+    c2p<M>(qm, wm, gm1);
+    c2p<M>(q0, w0, gm1);
+  }
+  for (int r = 0; r < TY; ++r) {
+    const int i = i0 + r;
+    if (i >= n0) break;  // whole warp
+    expand(nxt, qp);
+    if (r + 1 < TY) {  // the row after next, one row ahead of its use
+      const T* pn = row_ptr(i + 2);
+#pragma unroll
+      for (int s = 0; s < NV; ++s) nxt[s] = pn[s * plane];
+    }
+    c2p<M>(qp, wp, gm1);
+    // axis-1 neighbours from the adjacent lanes
+    T ql[8], qr[8], wl[8], wr[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { ql[k] = qr[k] = wl[k] = wr[k] = T(0); }
+#pragma unroll
+    for (int s = 0; s < NV; ++s) {
+      const int v = M::var(s);
+      ql[v] = __shfl_up_sync(FULL, q0[v], 1);
+      qr[v] = __shfl_down_sync(FULL, q0[v], 1);
+      wl[v] = __shfl_up_sync(FULL, w0[v], 1);
+      wr[v] = __shfl_down_sync(FULL, w0[v], 1);
+    }
+    if (out_lane) {
+      T dq0[8], dq1[8], dw0[8], dw1[8];  // second differences along axis 0 and axis 1
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        dq0[k] = (qp[k] - q0[k]) - (q0[k] - qm[k]);
+        dq1[k] = (qr[k] - q0[k]) - (q0[k] - ql[k]);
+        dw0[k] = (wp[k] - w0[k]) - (w0[k] - wm[k]);
+        dw1[k] = (wr[k] - w0[k]) - (w0[k] - wl[k]);
+      }
+      const long long g = (long long)i * n1 + j;
+      // axis-0 sweep: axis 0's correction first
+      {
+        T qq[8], wc[8], w[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          qq[k] = q0[k] - T(C24) * dq0[k];
+          wc[k] = T(C24) * dw0[k];
+          qq[k] = qq[k] - T(C24) * dq1[k];
+          wc[k] = wc[k] + T(C24) * dw1[k];
+        }
+        c2p<M>(qq, w, gm1);
+#pragma unroll
+        for (int s = 0; s < NV; ++s) w_ax0[s * plane + g] = w[M::var(s)] + wc[M::var(s)];
+      }
+      // axis-1 sweep: axis 1's correction first
+      if constexpr (cell_average_both_orders<T>()) {
+        T qq[8], wc[8], w[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          qq[k] = q0[k] - T(C24) * dq1[k];
+          wc[k] = T(C24) * dw1[k];
+          qq[k] = qq[k] - T(C24) * dq0[k];
+          wc[k] = wc[k] + T(C24) * dw0[k];
+        }
+        c2p<M>(qq, w, gm1);
+#pragma unroll
+        for (int s = 0; s < NV; ++s) w_ax1[s * plane + g] = w[M::var(s)] + wc[M::var(s)];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      qm[k] = q0[k]; q0[k] = qp[k];
+      wm[k] = w0[k]; w0[k] = wp[k];
+    }
+  }
+}
+
+template <typename T> using CellAvgFn = cudaError_t (*)(const T* q, T* w_ax0, T* w_ax1, int n0, int n1,
+                                                        long long plane, int bc, T gm1, const Clock* clk,
+                                                        cudaStream_t st);
+
+template <typename T, int MID>
+cudaError_t launch_cell_average(const T* q, T* w_ax0, T* w_ax1, int n0, int n1, long long plane, int bc, T gm1,
+                                const Clock* clk, cudaStream_t st) {
+  constexpr int TY = CellAvgTile<T, MID>::TY;
+  const dim3 grid((n1 + CA_W - 1) / CA_W, (n0 + TY * CA_WARPS - 1) / (TY * CA_WARPS));
+  cell_average_kernel<T, MID><<<grid, CA_NT, 0, st>>>(q, w_ax0, w_ax1, n0, n1, plane, bc, gm1, clk);
+  return cudaGetLastError();
+}
+
+// the launcher of a 2D model (4: Euler, 8: MHD / transverse velocities); nullptr otherwise.
+// Instantiated in cellavg_f32.cu (FMA, like the FP32 sweeps) and cellavg_f64.cu
+// (no FMA, like the FP64 sweeps).
+template <typename T> CellAvgFn<T> get_cell_average(int model) {
+  if (model == 4) return &launch_cell_average<T, 4>;
+  if (model == 8) return &launch_cell_average<T, 8>;
+  return nullptr;
+}
+
+extern template CellAvgFn<float> get_cell_average<float>(int);
+extern template CellAvgFn<double> get_cell_average<double>(int);
+
+}  // namespace astrea

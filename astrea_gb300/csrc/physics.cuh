@@ -107,9 +107,17 @@ template <class M> __device__ __noinline__ float internal_energy_fp64(float q0, 
 template <class M, typename T> __device__ __forceinline__ void c2p(const T* q, T* w, T gm1) {
   T rho = q[0];
   w[0] = rho;
-  w[1] = dvd(q[1], rho);
-  w[2] = M::VY ? dvd(q[2], rho) : T(0);
-  w[3] = M::VZ ? dvd(q[3], rho) : T(0);
+  if constexpr (Prec<T>::EXACT) {
+    w[1] = dvd(q[1], rho);
+    w[2] = M::VY ? dvd(q[2], rho) : T(0);
+    w[3] = M::VZ ? dvd(q[3], rho) : T(0);
+  } else {
+    // FP32: one reciprocal for the velocity components
+    const T inv = rho != T(0) ? T(1) / rho : T(0);
+    w[1] = q[1] * inv;
+    w[2] = M::VY ? q[2] * inv : T(0);
+    w[3] = M::VZ ? q[3] * inv : T(0);
+  }
   T kin = rho * nsq_vel<M>(w);
   T K = M::MHD ? T(.5) * (kin + nsq_mag<M>(q)) : T(.5) * kin;
   T e = q[4] - K;

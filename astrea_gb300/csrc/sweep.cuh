@@ -51,7 +51,9 @@ template <typename T> struct SweepArgs {
   int flatten;        // PPM: Colella (1990) flattening of the face values
   int viscosity;      // PPM: McCorquodale & Colella (2011) artificial viscosity added to the fluxes
   T av_alpha, av_beta;
-  const CUtensorMap* tmaps;  // optional (2D): TMA maps of q, indexed [axis][tile]; nullptr: plain loads
+  const CUtensorMap* tmaps;  // optional (2D): TMA maps of the staged level, indexed [axis][tile]; nullptr: plain loads
+  const T* ws;        // 2D high-order single-grid sweeps: the stage input's cell-averaged primitives in this
+                      // sweep's axis order (NV planes, from cell_average_kernel); they replace q's levels
 };
 
 // plane index of primitive variable v in model M (-1 if M does not store it)
@@ -86,7 +88,9 @@ template <int SCH, int DIM, int TS, int TT> struct Geom {
   static constexpr int QH = TT + 2 * QT, WH = TT + 2 * WT, RH = TT + 2 * RT, FH = TT + 2 * FT;
 };
 
-// The TMA box of a tile's staged state.  Axis 1 sweeps run along the contiguous
+// The TMA box of a tile's staged level: the cell-averaged primitives wS of the
+// high-order schemes, the state q of the others (whose q and wS levels have the
+// same extent).  Axis 1 sweeps run along the contiguous
 // axis (box x = sweep, y = rows), axis 0 sweeps across it (box x = rows, y =
 // sweep); the box's x origin is rounded down to 16 bytes and its x extent up to
 // 16 bytes, and XOFF is where the staged level starts inside the box's x.
@@ -97,25 +101,26 @@ template <typename T, int SCH, int DIM, int AX, int TS, int TT, int NV> struct T
   using G = Geom<SCH, DIM, TS, TT>;
   static constexpr int A = 16 / (int)sizeof(T);
   static constexpr bool DYN = AX == 0 && TT % A != 0;
-  static constexpr int XB = AX == 1 ? floor_to(G::Q_BEG, A) : floor_to(-G::QT, A);
-  static constexpr int BW = AX == 1 ? ceil_to(TS + G::Q_END - XB, A)
-                                    : (DYN ? ceil_to(G::QH + A - 1, A) : ceil_to(TT + G::QT - XB, A));
-  static constexpr int BH = AX == 1 ? G::QH : G::QW;
-  static constexpr int XOFF = AX == 1 ? G::Q_BEG - XB : -G::QT - XB;
+  static constexpr int XB = AX == 1 ? floor_to(G::W_BEG, A) : floor_to(-G::WT, A);
+  static constexpr int BW = AX == 1 ? ceil_to(TS + G::W_END - XB, A)
+                                    : (DYN ? ceil_to(G::WH + A - 1, A) : ceil_to(TT + G::WT - XB, A));
+  static constexpr int BH = AX == 1 ? G::WH : G::WW;
+  static constexpr int XOFF = AX == 1 ? G::W_BEG - XB : -G::WT - XB;
   static constexpr int BYTES = NV * BH * BW * (int)sizeof(T);
   static constexpr int TILE_ID = TT == 8 ? 0 : 1;
   static_assert(BW <= 256 && BH <= 256 && (BW * (int)sizeof(T)) % 16 == 0, "TMA box limits");
   // x origin of the box and the staged level's first column inside it, for the tile at (s0, t0)
   __host__ __device__ static int x0(int s0, int t0) {
     if (AX == 1) return s0 + XB;
-    return DYN ? ((t0 - G::QT) / A) * A : t0 + XB;  // t0 - QT >= 0 whenever the box is used
+    return DYN ? ((t0 - G::WT) / A) * A : t0 + XB;  // t0 - WT >= 0 whenever the box is used
   }
-  __host__ __device__ static int xoff(int t0) { return DYN ? (t0 - G::QT) - x0(0, t0) : XOFF; }
+  __host__ __device__ static int xoff(int t0) { return DYN ? (t0 - G::WT) - x0(0, t0) : XOFF; }
 };
 
-template <int SCH, int DIM, int TS, int TT, int NV> struct Smem {
+// WSIN: the tile stages the precomputed wS level and has no q level.
+template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Smem {
   using G = Geom<SCH, DIM, TS, TT>;
-  static constexpr int n_q = NV * G::QH * G::QW;
+  static constexpr int n_q = WSIN ? 0 : NV * G::QH * G::QW;
   static constexpr int n_qw = G::HO ? n_q : 0;
   static constexpr int n_face = DIM == 2 ? 5 * NV * G::FH * G::KW : 0;
   static constexpr int n_F = NV * TT * G::KW;
@@ -140,7 +145,14 @@ template <int SCH, int DIM, int TS, int TT, int NV> struct Smem {
   static constexpr int MU_OFF = MU_IN_F ? FA_OFF + n_face : base;
   static constexpr int ETA_OFF = ETA_IN_GAP ? n_q + n_qw : base + (MU_IN_F ? 0 : n_mu);
   static constexpr int CB_OFF = ETA_OFF + n_eta;
-  static constexpr int total = base + (MU_IN_F ? 0 : n_mu) + (ETA_IN_GAP ? 0 : n_eta + n_cb);
+  static constexpr int total0 = base + (MU_IN_F ? 0 : n_mu) + (ETA_IN_GAP ? 0 : n_eta + n_cb);
+  // WSIN PPM tiles: the state on the viscous faces' cells (columns [s0-1, s0+TS], the
+  // tile's rows), staged for the viscous fluxes, after the coefficients when it fits
+  static constexpr int QSW = TS + 2;
+  static constexpr int n_qs = (WSIN && SCH == PPM) ? NV * TT * QSW : 0;
+  static constexpr bool QS_IN_GAP = ETA_IN_GAP && (n_q + n_qw + n_eta + n_cb + n_qs <= FA_OFF + n_face);
+  static constexpr int QS_OFF = QS_IN_GAP ? CB_OFF + n_cb : total0;
+  static constexpr int total = total0 + (QS_IN_GAP ? 0 : n_qs);
 };
 
 template <class M, typename T> __device__ __forceinline__ void load_sm(const T* base, int stride, int idx, T* x) {
@@ -195,13 +207,18 @@ template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, un
 
 // One tile: cells [s0, s0+TS) along the sweep and rows [t0, t0+TT) across it.
 // Called by the single-grid kernel (one tile per CTA) and by the batched
-// persistent kernel (a work list of tiles of many grids).
-template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, bool CL, int NT, bool TMA = false>
+// persistent kernel (a work list of tiles of many grids).  WSIN: the tile
+// stages the precomputed cell-averaged primitives a.ws instead of forming them
+// from the state (2D high-order schemes, single-grid kernel).
+template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, bool CL, int NT, bool TMA = false,
+          bool WSIN = false>
 __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int s0, const int t0,
                                                 unsigned char* __restrict__ smem_raw) {
   using M = Model<MID>;
   using G = Geom<SCH, DIM, TS, TT>;
-  using S = Smem<SCH, DIM, TS, TT, M::NV>;
+  using S = Smem<SCH, DIM, TS, TT, M::NV, WSIN>;
+  static_assert(!WSIN || (DIM == 2 && G::HO), "precomputed wS is for 2D high-order tiles");
+  static_assert(!TMA || WSIN || !G::HO, "the TMA box holds the wS level: high-order tiles stage it precomputed");
   constexpr int NV = M::NV;
   T* sm = reinterpret_cast<T*>(smem_raw);
   T* s_q = sm;                       // region 0 (a): q and its point primitives
@@ -233,8 +250,75 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     return AX == 0 ? (long long)gs * a.n1 + gt : (long long)gt * a.n1 + gs;
   };
 
-  // ---- level q: conservative state with halos (input boundary map), and its point primitives
-  if constexpr (TMA) {
+  // element (gs, gt) of a grid-sized input, at a virtual index served by the boundary map
+  auto gmap = [&](int v, int n) -> int { return (v >= 0 && v < n) ? v : bc_map(v, n, a.bc); };
+
+  if constexpr (WSIN) {
+    // ---- level wS, staged: the cell-averaged primitives of the stage input, precomputed
+    // for this sweep's axis order (the same values levels q and wS form below)
+    constexpr int W = G::WW, H = G::WH;
+    // PPM with viscosity: the state on the cells either side of the tile's interfaces, for
+    // the viscous fluxes (in the bulk-copy path its loads overlap the copy)
+    auto stage_strip = [&]() {
+      if constexpr (SCH == PPM) {
+        if (a.viscosity) {
+          constexpr int QW = S::QSW;
+          T* s_qs = sm + S::QS_OFF;
+          for (int e = tid; e < QW * TT; e += nth) {
+            int row, col;
+            if (AX == 0) { row = e % TT; col = e / TT; } else { col = e % QW; row = e / QW; }
+            const long long g = gidx(gmap(s0 - 1 + col, Ns), gmap(t0 + row, Nt));
+#pragma unroll
+            for (int s = 0; s < NV; ++s) s_qs[(s * TT + row) * QW + col] = a.q[s * a.plane + g];
+          }
+        }
+      }
+    };
+    if constexpr (TMA) {
+      using B = TmaBox<T, SCH, DIM, AX, TS, TT, NV>;
+      __shared__ unsigned long long s_bar;
+      T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_R) + 127) & ~uintptr_t(127));
+      if (tid == 0) {
+        mbar_init(&s_bar, 1);
+        mbar_fence_init();
+        mbar_arrive_expect_tx(&s_bar, (unsigned)B::BYTES);
+        const CUtensorMap* map = a.tmaps + (AX * 2 + B::TILE_ID);
+        if (AX == 1) tma_load_3d(stage, map, B::x0(s0, t0), t0 - G::WT, 0, &s_bar);
+        else tma_load_3d(stage, map, B::x0(s0, t0), s0 + G::W_BEG, 0, &s_bar);
+      }
+      __syncthreads();  // the barrier is initialised before anyone waits on it
+      stage_strip();
+      constexpr int kWaitLimit = 1 << 16;
+      const bool landed = mbar_wait_bounded(&s_bar, 0, kWaitLimit);
+      if (!__syncthreads_and(landed)) {
+        // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
+        if (tid == 0) {
+          atomicOr(&a.clock->status, 2);
+          mbar_wait_bounded(&s_bar, 0, kWaitLimit);
+        }
+        return;
+      }
+      const int xo = B::xoff(t0);
+      for (int e = tid; e < W * H; e += nth) {
+        int row, col;
+        if (AX == 0) { row = e % H; col = e / H; } else { col = e % W; row = e / W; }
+#pragma unroll
+        for (int s = 0; s < NV; ++s)
+          s_w[(s * H + row) * W + col] = AX == 1 ? stage[(s * B::BH + row) * B::BW + col + xo]
+                                                 : stage[(s * B::BH + col) * B::BW + row + xo];
+      }
+    } else {
+      for (int e = tid; e < W * H; e += nth) {
+        int row, col;
+        if (AX == 0) { row = e % H; col = e / H; } else { col = e % W; row = e / W; }
+        const long long g = gidx(gmap(s0 + G::W_BEG + col, Ns), gmap(t0 - G::WT + row, Nt));
+#pragma unroll
+        for (int s = 0; s < NV; ++s) s_w[(s * H + row) * W + col] = a.ws[s * a.plane + g];
+      }
+      stage_strip();
+    }
+  } else if constexpr (TMA) {
+    // ---- level q: conservative state with halos (input boundary map), and its point primitives;
     // one thread issues the bulk copy of the whole box into the (still unused) R region
     using B = TmaBox<T, SCH, DIM, AX, TS, TT, NV>;
     __shared__ unsigned long long s_bar;
@@ -306,7 +390,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   // ---- level wS: cell-averaged primitives
   // (items laid out with the staged level's row pitch, so that a warp's loads
   // stay in consecutive banks across a row change; the two extra columns idle)
-  {
+  if constexpr (!WSIN) {
     constexpr int W = G::WW, H = G::WH, QW = G::QW, QH = G::QH;
     for (int e = tid; e < QW * H; e += nth) {
       const int row = e / QW, col = e % QW;
@@ -353,8 +437,8 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       }
       store_sm<M>(s_w, H * W, row * W + col, w);
     }
+    __syncthreads();
   }
-  __syncthreads();
 
   // ---- PPM extras (optional): flattening coefficients (ppm.apply_flattener,
   // ppm.py:111-134) and artificial-viscosity face fluxes (ppm.apply_artificial_viscosity,
@@ -434,11 +518,21 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
             const T cmin = npmin(cs_x, cs_xp);
             nu = npmin(T(1), dvd(lam * lam, a.av_beta * (cmin * cmin))) * lam;
           }
-          const T* qrow = s_q + (rt - (t0 - G::QT)) * G::QW - (s0 + G::Q_BEG);
+          if constexpr (WSIN) {
+            // x, xp lie in [s0-1, s0+TS] and rt in [t0, t0+TT) (clamped or not): the staged strip
+            const T* qrow = sm + S::QS_OFF + (rt - t0) * S::QSW - (s0 - 1);
 #pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            const T* qv = qrow + v * G::QH * G::QW;
-            s_mu[(v * TT + row) * W + col] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+            for (int v = 0; v < NV; ++v) {
+              const T* qv = qrow + v * TT * S::QSW;
+              s_mu[(v * TT + row) * W + col] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+            }
+          } else {
+            const T* qrow = s_q + (rt - (t0 - G::QT)) * G::QW - (s0 + G::Q_BEG);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+              const T* qv = qrow + v * G::QH * G::QW;
+              s_mu[(v * TT + row) * W + col] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+            }
           }
         }
       }
@@ -723,36 +817,40 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 }
 
 // Clamping is only needed on outflow grids, for tiles whose widest level
-// (the staged state) reaches past the grid edge.  With TMA (single-grid 2D
-// kernels), tiles whose whole TMA box lies inside the grid are staged by the
-// bulk copy; the others load per thread as without it.
+// (the staged state, or the staged wS under WSIN) reaches past the grid edge.
+// With TMA (single-grid 2D kernels), tiles whose whole TMA box lies inside the
+// grid are staged by the bulk copy; the others load per thread as without it.
 template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT = (DIM == 1 ? 64 : 256),
-          bool TMA_OK = false>
+          bool TMA_OK = false, bool WSIN = false>
 __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, const int t0,
                                            unsigned char* __restrict__ smem_raw) {
   using G = Geom<SCH, DIM, TS, TT>;
-  using S = Smem<SCH, DIM, TS, TT, Model<MID>::NV>;
+  using S = Smem<SCH, DIM, TS, TT, Model<MID>::NV, WSIN>;
   const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
   const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
-  if constexpr (TMA_OK && DIM == 2) {
+  if constexpr (TMA_OK && DIM == 2 && (WSIN || !G::HO)) {
     using B = TmaBox<T, SCH, DIM, AX, TS, TT, Model<MID>::NV>;
     if constexpr ((size_t)S::n_R * sizeof(T) >= (size_t)B::BYTES + 128) {
       const bool box_in = a.tmaps != nullptr &&
-                          (AX == 1 ? (s0 + B::XB >= 0 && s0 + B::XB + B::BW <= a.n1 && t0 - G::QT >= 0 &&
-                                      t0 - G::QT + B::BH <= a.n0)
-                                   : (t0 - G::QT >= 0 && B::x0(s0, t0) + B::BW <= a.n1 && s0 + G::Q_BEG >= 0 &&
-                                      s0 + G::Q_BEG + B::BH <= a.n0));
+                          (AX == 1 ? (s0 + B::XB >= 0 && s0 + B::XB + B::BW <= a.n1 && t0 - G::WT >= 0 &&
+                                      t0 - G::WT + B::BH <= a.n0)
+                                   : (t0 - G::WT >= 0 && B::x0(s0, t0) + B::BW <= a.n1 && s0 + G::W_BEG >= 0 &&
+                                      s0 + G::W_BEG + B::BH <= a.n0));
       if (box_in) {
-        sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, true>(a, s0, t0, smem_raw);
+        sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, true, WSIN>(a, s0, t0, smem_raw);
         return;
       }
     }
   }
-  const bool inside = s0 + G::Q_BEG >= 0 && s0 + TS + G::Q_END <= Ns &&
-                      (DIM == 1 || (t0 - G::QT >= 0 && t0 + TT + G::QT <= Nt));
-  if (a.bc == EDGE && !inside) sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, true, NT>(a, s0, t0, smem_raw);
-  else sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT>(a, s0, t0, smem_raw);
+  constexpr int BEG = WSIN ? G::W_BEG : G::Q_BEG, END = WSIN ? G::W_END : G::Q_END, HT = WSIN ? G::WT : G::QT;
+  const bool inside = s0 + BEG >= 0 && s0 + TS + END <= Ns && (DIM == 1 || (t0 - HT >= 0 && t0 + TT + HT <= Nt));
+  if (a.bc == EDGE && !inside)
+    sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, true, NT, false, WSIN>(a, s0, t0, smem_raw);
+  else sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, false, WSIN>(a, s0, t0, smem_raw);
 }
+
+// The single-grid kernels of 2D high-order schemes stage the precomputed wS.
+template <int SCH, int DIM> constexpr bool sweep_wsin() { return DIM == 2 && SCH >= PPM; }
 
 // FP32 Euler tiles fit 1024 threads per SM (<= 64 registers); FP64 and MHD tiles are larger
 template <typename T, int MID, int NT> struct SweepOcc {
@@ -763,7 +861,8 @@ template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT
 __global__ void __launch_bounds__(NT, (SweepOcc<T, MID, NT>::value)) sweep_kernel(const SweepArgs<T> a) {
   if (a.clock->done) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT, NT, true>(a, blockIdx.x * TS, blockIdx.y * TT, smem_raw);
+  sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT, NT, true, sweep_wsin<SCH, DIM>()>(a, blockIdx.x * TS, blockIdx.y * TT,
+                                                                               smem_raw);
 }
 
 }  // namespace astrea

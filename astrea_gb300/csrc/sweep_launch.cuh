@@ -20,7 +20,7 @@ template <> struct Tile2<0> { static constexpr int TS = 32, TT = 8, NT = 256; };
 template <> struct Tile2<1> { static constexpr int TS = 32, TT = 15, NT = 512; };
 
 template <typename T, int MID, int SCH, int DIM, int TS, int TT> constexpr size_t sweep_smem_bytes() {
-  return sizeof(T) * (size_t)Smem<SCH, DIM, TS, TT, Model<MID>::NV>::total;
+  return sizeof(T) * (size_t)Smem<SCH, DIM, TS, TT, Model<MID>::NV, sweep_wsin<SCH, DIM>()>::total;
 }
 
 template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT>

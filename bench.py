@@ -472,8 +472,8 @@ def main():
     s32.step(args.warmup, graph=True)
     torch.cuda.synchronize()
     barrier(ws)
-    kernel_ms = (ctypes.c_double * 3)()
-    launches = (ctypes.c_int * 3)()
+    kernel_ms = (ctypes.c_double * 4)()
+    launches = (ctypes.c_int * 4)()
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as cs:
@@ -490,11 +490,13 @@ def main():
     tiles32 = s32.sweep_tiles()
 
     # roofline of the sweep kernel: algorithmic bytes per launch / mean launch time.
-    # Per step: stage 0 two sweeps read the state and write a divergence (2*C*s per cell each);
-    # stages 1-2: the first sweep the same, the second reads state, divergence and u0 and writes
-    # the stage result (4*C*s).  C = 4 stored variables, s = 4 bytes.
+    # Per stage a pre-pass reads the stage state and writes its cell averages for both sweep
+    # orders (3*C*s per cell); each sweep reads its cell averages and writes a divergence
+    # (2*C*s), except the second sweep of stages 1-2, which reads its cell averages, the other
+    # divergence, u0 and the stage state and writes the stage result (5*C*s).
+    # C = 4 stored variables, s = 4 bytes.
     C, sz = 4, 4
-    alg_bytes_step = cells * C * sz * (2 + 2 + (2 + 4) + (2 + 4))
+    alg_bytes_step = cells * C * sz * (2 + 2 + (2 + 5) + (2 + 5))
     sweep_launches = max(launches[0], 1)
     alg_per_launch = alg_bytes_step * args.steps / sweep_launches
     achieved = alg_per_launch / (kernel_ms[0] / sweep_launches / 1e3) / 1e9
@@ -505,6 +507,11 @@ def main():
                 "kernel": "sweep_kernel (every sweep launch of the timed steps)", "peak_source": peak_kind,
                 "alg_bytes_per_launch": alg_per_launch, "step_frac": step_alg * (value / ws) / cells / 1e9 / peak,
                 "note": "ALU/issue-bound stencil: thousands of FP32 ops per cell-update against 128 B"}
+    if launches[3]:
+        ca_bytes = cells * C * sz * 3
+        roofline["cell_average_prepass"] = {"launches": launches[3], "ms": kernel_ms[3],
+                                            "achieved_gbs": ca_bytes / (kernel_ms[3] / launches[3] / 1e3) / 1e9,
+                                            "alg_bytes_per_launch": ca_bytes}
 
     if args.only_fp32:
         if rank == 0:
@@ -512,7 +519,8 @@ def main():
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                               "config": {"workload": WORKLOAD, "cells": cells}, "only_fp32": True,
                               "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1],
-                                            "bookkeeping": kernel_ms[2]}, "roofline": roofline}), flush=True)
+                                            "bookkeeping": kernel_ms[2], "cell_average": kernel_ms[3]},
+                              "roofline": roofline}), flush=True)
         return 0
 
     # ---- FP64 plain, same workload
@@ -601,9 +609,10 @@ def main():
             "fp32_over_fp64": value / ws / value64,
             "l1_rho_fp32_vs_fp64": l1, "l1_after_steps": k,
             "roofline": roofline,
-            "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1], "bookkeeping": kernel_ms[2]},
-            "gpu_launches": launches[0] + launches[1] + launches[2],
-            "launches_per_step": (launches[0] + launches[1] + launches[2]) / args.steps,
+            "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1], "bookkeeping": kernel_ms[2],
+                          "cell_average": kernel_ms[3]},
+            "gpu_launches": sum(launches),
+            "launches_per_step": sum(launches) / args.steps,
             "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
                     "d2h_bytes_per_step": state_bytes, "steps": args.e2e_steps},
             "batched": batched,

@@ -123,10 +123,12 @@ int astrea_step(astrea_handle* h, void* state, int nsteps, void* stream);
 int astrea_graph_step(astrea_handle* h, void* state, int nsteps, void* stream);
 
 /* Same as astrea_step, with a CUDA event pair recorded on ``stream`` around
- * every kernel launch.  kernel_ms[k] / launches[k] receive the summed device
- * time and the launch count per kernel kind k: 0 sweep, 1 stage-0 combine,
- * 2 dt and step bookkeeping.  Synchronises ``stream``.  (Instrumentation for
- * measurement; no counterpart in the reference.) */
+ * every kernel launch.  kernel_ms[k] / launches[k] (4 entries each) receive
+ * the summed device time and the launch count per kernel kind k: 0 sweep,
+ * 1 stage combine (stage 0; the register integrators' stage kernel; the
+ * constrained-transport kernels), 2 dt and step bookkeeping, 3 the
+ * cell-average pre-pass of 2D high-order schemes.  Synchronises ``stream``.
+ * (Instrumentation for measurement; no counterpart in the reference.) */
 int astrea_step_timed(astrea_handle* h, void* state, int nsteps, double* kernel_ms, int* launches, void* stream);
 
 /* The sweep tile in use along ``axis`` (cells along the sweep x rows across it).

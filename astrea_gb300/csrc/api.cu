@@ -17,6 +17,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/astrea_gb300.h"
@@ -147,7 +148,23 @@ template <typename T, int SCH> static void box_of(int ax, int tile, cuuint32_t* 
     else { *bw = B1::BW; *bh = B1::BH; }
   }
 }
-template <typename T> static void box_for(int scheme, int ax, int tile, cuuint32_t* bw, cuuint32_t* bh) {
+// the viscous strip box (StripBox) of (axis, tile)
+template <typename T> static void strip_box(int ax, int tile, cuuint32_t* bw, cuuint32_t* bh) {
+  if (ax == 0) {
+    using B0 = StripBox<T, 0, Tile2<0>::TS, Tile2<0>::TT>;
+    using B1 = StripBox<T, 0, Tile2<1>::TS, Tile2<1>::TT>;
+    if (tile == 0) { *bw = B0::BW; *bh = B0::BH; }
+    else { *bw = B1::BW; *bh = B1::BH; }
+  } else {
+    using B0 = StripBox<T, 1, Tile2<0>::TS, Tile2<0>::TT>;
+    using B1 = StripBox<T, 1, Tile2<1>::TS, Tile2<1>::TT>;
+    if (tile == 0) { *bw = B0::BW; *bh = B0::BH; }
+    else { *bw = B1::BW; *bh = B1::BH; }
+  }
+}
+// kind 0: the staged level's box of ``scheme``; kind 1: the viscous strip's box
+template <typename T> static void box_for(int scheme, int kind, int ax, int tile, cuuint32_t* bw, cuuint32_t* bh) {
+  if (kind == 1) return strip_box<T>(ax, tile, bw, bh);
   switch (scheme) {
     case PCM: box_of<T, PCM>(ax, tile, bw, bh); break;
     case PLM: box_of<T, PLM>(ax, tile, bw, bh); break;
@@ -173,9 +190,10 @@ template <typename T> struct Engine final : IEngine {
   T* wsb[2] = {nullptr, nullptr};    // 2D high-order schemes: the stage input's cell averages, one per sweep order
   CellAvgFn<T> cavg = nullptr;
   // TMA maps of every buffer a sweep reads (state, stage buffers, registers): 4 per buffer ([axis][tile])
+  // (kind 0: the staged level's box; kind 1: the viscous strip's box, for the stage inputs of PPM with viscosity)
   static constexpr int kMapSlots = 16;
   CUtensorMap* d_maps = nullptr;
-  std::vector<const void*> map_ptr;
+  std::vector<std::pair<const void*, int>> map_ptr;
   SweepFn<T> cand[2][NTILES2] = {};  // tile candidates per axis (nullptr: not built for this configuration)
   int tile[2] = {0, 0};
   bool tuned = false;
@@ -243,6 +261,11 @@ template <typename T> struct Engine final : IEngine {
       CK(cudaMalloc(&d_maps, sizeof(CUtensorMap) * 4 * kMapSlots));
       if (use_ws()) {
         for (int i = 0; i < n_ws(); ++i) CK(add_map(wsb[i]));
+        if (strip_maps()) {
+          for (int i = 0; i < 2; ++i) CK(add_map(k[i], 1));
+          for (T* r : reg)
+            if (r) CK(add_map(r, 1));
+        }
       } else {
         for (int i = 0; i < 2; ++i) CK(add_map(k[i]));
         for (T* r : reg)
@@ -258,9 +281,12 @@ template <typename T> struct Engine final : IEngine {
     return ASTREA_OK;
   }
 
+  // the stage inputs of PPM with viscosity get strip maps
+  bool strip_maps() const { return use_ws() && cfg.scheme == PPM && (cfg.flags & ASTREA_FLAG_VISCOSITY) != 0; }
+
   // encode the four TMA maps of a buffer (synchronous; outside any capture)
-  cudaError_t add_map(const void* p) {
-    if (!d_maps || !p || find_map(p) || (int)map_ptr.size() >= kMapSlots) return cudaSuccess;
+  cudaError_t add_map(const void* p, int kind = 0) {
+    if (!d_maps || !p || find_map(p, kind) || (int)map_ptr.size() >= kMapSlots) return cudaSuccess;
     if ((reinterpret_cast<uintptr_t>(p) & 15) != 0) return cudaSuccess;
     CUtensorMap m[4];
     const cuuint64_t dims[3] = {(cuuint64_t)cfg.n1, (cuuint64_t)cfg.n0, (cuuint64_t)nv};
@@ -269,7 +295,7 @@ template <typename T> struct Engine final : IEngine {
     for (int ax = 0; ax < 2; ++ax)
       for (int tile = 0; tile < 2; ++tile) {
         cuuint32_t box[3] = {0, 0, (cuuint32_t)nv};
-        box_for<T>(cfg.scheme, ax, tile, &box[0], &box[1]);
+        box_for<T>(cfg.scheme, kind, ax, tile, &box[0], &box[1]);
         const CUresult r = encode_tiled()(&m[ax * 2 + tile], sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
                                                                              : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
                                           3, const_cast<void*>(p), dims, strides, box, estr,
@@ -279,19 +305,22 @@ template <typename T> struct Engine final : IEngine {
       }
     cudaError_t e = cudaMemcpy(d_maps + 4 * map_ptr.size(), m, sizeof(m), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return e;
-    map_ptr.push_back(p);
+    map_ptr.push_back({p, kind});
     return cudaSuccess;
   }
-  const CUtensorMap* find_map(const void* p) const {
+  const CUtensorMap* find_map(const void* p, int kind = 0) const {
     for (size_t i = 0; i < map_ptr.size(); ++i)
-      if (map_ptr[i] == p) return d_maps + 4 * i;
+      if (map_ptr[i].first == p && map_ptr[i].second == kind) return d_maps + 4 * i;
     return nullptr;
   }
 
   int prepare(const void* state, cudaStream_t st) override {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     CK(cudaStreamIsCapturing(st, &cs));
-    if (cs == cudaStreamCaptureStatusNone && !use_ws()) CK(add_map(state));
+    if (cs == cudaStreamCaptureStatusNone) {
+      if (!use_ws()) CK(add_map(state));
+      else if (strip_maps()) CK(add_map(state, 1));
+    }
     return tune(state, st);
   }
 
@@ -380,6 +409,7 @@ template <typename T> struct Engine final : IEngine {
     a.av_alpha = T(0.3);
     a.av_beta = T(0.3);
     a.tmaps = use_ws() ? nullptr : find_map(q);
+    a.qmaps = strip_maps() ? find_map(q, 1) : nullptr;
     return a;
   }
 

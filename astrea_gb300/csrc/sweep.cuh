@@ -54,6 +54,7 @@ template <typename T> struct SweepArgs {
   const CUtensorMap* tmaps;  // optional (2D): TMA maps of the staged level, indexed [axis][tile]; nullptr: plain loads
   const T* ws;        // 2D high-order single-grid sweeps: the stage input's cell-averaged primitives in this
                       // sweep's axis order (NV planes, from cell_average_kernel); they replace q's levels
+  const CUtensorMap* qmaps;  // optional (with ws): TMA maps of q for the viscous strip (StripBox), [axis][tile]
 };
 
 // plane index of primitive variable v in model M (-1 if M does not store it)
@@ -117,6 +118,29 @@ template <typename T, int SCH, int DIM, int AX, int TS, int TT, int NV> struct T
   __host__ __device__ static int xoff(int t0) { return DYN ? (t0 - G::WT) - x0(0, t0) : XOFF; }
 };
 
+// The TMA box of the viscous strip of a WSIN PPM tile: the state on cells
+// [s0-1, s0+TS] along the sweep and rows [t0, t0+TT) across it, with the box's
+// x origin rounded down and its x extent up to 16 bytes (as TmaBox).
+template <typename T, int AX, int TS, int TT> struct StripBox {
+  static constexpr int A = 16 / (int)sizeof(T);
+  static constexpr bool DYN = AX == 0 && TT % A != 0;
+  static constexpr int BW = AX == 1 ? ceil_to(TS + 1 + A, A) : (DYN ? ceil_to(TT + A - 1, A) : TT);
+  static constexpr int BH = AX == 1 ? TT : TS + 2;
+  static constexpr int TILE_ID = TT == 8 ? 0 : 1;
+  static_assert(BW <= 256 && BH <= 256 && (BW * (int)sizeof(T)) % 16 == 0, "TMA box limits");
+  __host__ __device__ static int x0(int s0, int t0) { return AX == 1 ? s0 - A : (DYN ? (t0 / A) * A : t0); }
+  __host__ __device__ static int y0(int s0, int t0) { return AX == 1 ? t0 : s0 - 1; }
+  // the box lies inside an n0 x n1 grid
+  __host__ __device__ static bool inside(int s0, int t0, int n0, int n1) {
+    return AX == 1 ? (s0 - A >= 0 && s0 - A + BW <= n1 && t0 + TT <= n0)
+                   : (x0(s0, t0) + BW <= n1 && s0 - 1 >= 0 && s0 - 1 + BH <= n0);
+  }
+  // element of plane v, cell x along the sweep (in [s0-1, s0+TS]), row rt (in [t0, t0+TT))
+  __host__ __device__ static int at(int v, int x, int rt, int s0, int t0) {
+    return AX == 1 ? (v * BH + (rt - t0)) * BW + (x - (s0 - A)) : (v * BH + (x - (s0 - 1))) * BW + (rt - x0(s0, t0));
+  }
+};
+
 // WSIN: the tile stages the precomputed wS level and has no q level.
 template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Smem {
   using G = Geom<SCH, DIM, TS, TT>;
@@ -148,8 +172,10 @@ template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Sm
   static constexpr int total0 = base + (MU_IN_F ? 0 : n_mu) + (ETA_IN_GAP ? 0 : n_eta + n_cb);
   // WSIN PPM tiles: the state on the viscous faces' cells (columns [s0-1, s0+TS], the
   // tile's rows), staged for the viscous fluxes, after the coefficients when it fits
+  // (per-thread layout [NV][TT][TS+2], or a StripBox of either axis plus 128 bytes of alignment)
   static constexpr int QSW = TS + 2;
-  static constexpr int n_qs = (WSIN && SCH == PPM) ? NV * TT * QSW : 0;
+  static constexpr int n_qs_box = NV * ((TS + 8) * TT > (TT + 6) * (TS + 2) ? (TS + 8) * TT : (TT + 6) * (TS + 2)) + 32;
+  static constexpr int n_qs = (WSIN && SCH == PPM) ? (NV * TT * QSW > n_qs_box ? NV * TT * QSW : n_qs_box) : 0;
   static constexpr bool QS_IN_GAP = ETA_IN_GAP && (n_q + n_qw + n_eta + n_cb + n_qs <= FA_OFF + n_face);
   static constexpr int QS_OFF = QS_IN_GAP ? CB_OFF + n_cb : total0;
   static constexpr int total = total0 + (QS_IN_GAP ? 0 : n_qs);
@@ -252,13 +278,23 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 
   // element (gs, gt) of a grid-sized input, at a virtual index served by the boundary map
   auto gmap = [&](int v, int n) -> int { return (v >= 0 && v < n) ? v : bc_map(v, n, a.bc); };
+  // WSIN PPM tiles with viscosity: the viscous strip arrives by bulk copy (same for the whole CTA)
+  bool strip_tma = false;
+  T* qs_box = nullptr;
+  if constexpr (WSIN && TMA && SCH == PPM) {
+    using SB = StripBox<T, AX, TS, TT>;
+    static_assert(NV * SB::BH * SB::BW + 128 / (int)sizeof(T) <= S::n_qs, "viscous strip box exceeds its region");
+    strip_tma = a.viscosity && a.qmaps != nullptr && SB::inside(s0, t0, a.n0, a.n1);
+    qs_box = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(sm + S::QS_OFF) + 127) & ~uintptr_t(127));
+  }
 
   if constexpr (WSIN) {
     // ---- level wS, staged: the cell-averaged primitives of the stage input, precomputed
     // for this sweep's axis order (the same values levels q and wS form below)
     constexpr int W = G::WW, H = G::WH;
     // PPM with viscosity: the state on the cells either side of the tile's interfaces, for
-    // the viscous fluxes (in the bulk-copy path its loads overlap the copy)
+    // the viscous fluxes: a second bulk copy beside the wS box when both lie inside the grid,
+    // else per-thread loads (in the bulk-copy path their loads overlap the copy)
     auto stage_strip = [&]() {
       if constexpr (SCH == PPM) {
         if (a.viscosity) {
@@ -276,18 +312,22 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     };
     if constexpr (TMA) {
       using B = TmaBox<T, SCH, DIM, AX, TS, TT, NV>;
+      using SB = StripBox<T, AX, TS, TT>;
       __shared__ unsigned long long s_bar;
       T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_R) + 127) & ~uintptr_t(127));
       if (tid == 0) {
         mbar_init(&s_bar, 1);
         mbar_fence_init();
-        mbar_arrive_expect_tx(&s_bar, (unsigned)B::BYTES);
+        unsigned bytes = (unsigned)B::BYTES;
+        if (strip_tma) bytes += (unsigned)(NV * SB::BH * SB::BW * (int)sizeof(T));
+        mbar_arrive_expect_tx(&s_bar, bytes);
         const CUtensorMap* map = a.tmaps + (AX * 2 + B::TILE_ID);
         if (AX == 1) tma_load_3d(stage, map, B::x0(s0, t0), t0 - G::WT, 0, &s_bar);
         else tma_load_3d(stage, map, B::x0(s0, t0), s0 + G::W_BEG, 0, &s_bar);
+        if (strip_tma) tma_load_3d(qs_box, a.qmaps + (AX * 2 + SB::TILE_ID), SB::x0(s0, t0), SB::y0(s0, t0), 0, &s_bar);
       }
       __syncthreads();  // the barrier is initialised before anyone waits on it
-      stage_strip();
+      if (!strip_tma) stage_strip();
       constexpr int kWaitLimit = 1 << 16;
       const bool landed = mbar_wait_bounded(&s_bar, 0, kWaitLimit);
       if (!__syncthreads_and(landed)) {
@@ -520,11 +560,19 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
           }
           if constexpr (WSIN) {
             // x, xp lie in [s0-1, s0+TS] and rt in [t0, t0+TT) (clamped or not): the staged strip
-            const T* qrow = sm + S::QS_OFF + (rt - t0) * S::QSW - (s0 - 1);
+            if (strip_tma) {
+              using SB = StripBox<T, AX, TS, TT>;
 #pragma unroll
-            for (int v = 0; v < NV; ++v) {
-              const T* qv = qrow + v * TT * S::QSW;
-              s_mu[(v * TT + row) * W + col] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+              for (int v = 0; v < NV; ++v)
+                s_mu[(v * TT + row) * W + col] =
+                    a.av_alpha * (nu * (qs_box[SB::at(v, xp, rt, s0, t0)] - qs_box[SB::at(v, x, rt, s0, t0)]));
+            } else {
+              const T* qrow = sm + S::QS_OFF + (rt - t0) * S::QSW - (s0 - 1);
+#pragma unroll
+              for (int v = 0; v < NV; ++v) {
+                const T* qv = qrow + v * TT * S::QSW;
+                s_mu[(v * TT + row) * W + col] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+              }
             }
           } else {
             const T* qrow = s_q + (rt - (t0 - G::QT)) * G::QW - (s0 + G::Q_BEG);

@@ -48,18 +48,22 @@ def run(cfg, w, steps, tma):
             os.environ["ASTREA_TMA"] = old
 
 
-def cfg_of(n, precision, scheme, solver, bc):
+def cfg_of(n, precision, scheme, solver, bc, dissipation=False):
     return RunConfig(dim=2, n0=n, n1=n, model=4, precision=precision, scheme=scheme, solver=solver,
-                     integrator="ssprk33", boundary=bc, gamma=1.4, dx=1.0 / n, cfl=0.4, t_end=1.0, compat=False)
+                     integrator="ssprk33", boundary=bc, gamma=1.4, dx=1.0 / n, cfl=0.4, t_end=1.0, compat=False,
+                     flatten=dissipation, viscosity=dissipation)
 
 
+# PPM with flattening and viscosity also copies the viscous faces' state strip in bulk
 @pytest.mark.parametrize("precision", [64, 32])
-@pytest.mark.parametrize("scheme,solver,bc", [("ppm", "hllc", "edge"), ("plm", "llf", "wrap"), ("weno5", "hllc", "wrap")])
-def test_tma_equals_plain_loads(precision, scheme, solver, bc):
+@pytest.mark.parametrize("scheme,solver,bc,dissipation", [("ppm", "hllc", "edge", False), ("plm", "llf", "wrap", False),
+                                                          ("weno5", "hllc", "wrap", False),
+                                                          ("ppm", "hllc", "wrap", True), ("ppm", "llf", "edge", True)])
+def test_tma_equals_plain_loads(precision, scheme, solver, bc, dissipation):
     n = 128
     w = quadrants(n)
-    a = run(cfg_of(n, precision, scheme, solver, bc), w, 3, True)
-    b = run(cfg_of(n, precision, scheme, solver, bc), w, 3, False)
+    a = run(cfg_of(n, precision, scheme, solver, bc, dissipation), w, 3, True)
+    b = run(cfg_of(n, precision, scheme, solver, bc, dissipation), w, 3, False)
     assert np.array_equal(a, b)
 
 

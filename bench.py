@@ -48,9 +48,9 @@ WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc) with flattening and ar
 # Mean DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per sweep launch
 # over the SSPRK3 steps of the headline FP32 workload at 2048^2, from one ncu
 # launch list (profiles/sweep_kernel_f32_ppm_hllc_2d.md); scaled by cells for
-# other sizes.  Below the algorithmic bytes because the L2 keeps part of each
-# stage's output for the next launch.
-SWEEP_DRAM_BYTES = 146.6e6
+# other sizes.  Slightly above the algorithmic bytes: the viscous strip reads
+# the stage state once more besides its cell averages.
+SWEEP_DRAM_BYTES = 218.6e6
 SWEEP_DRAM_CELLS = 2048 * 2048
 
 
@@ -490,10 +490,10 @@ def main():
     tiles32 = s32.sweep_tiles()
 
     # roofline of the sweep kernel: algorithmic bytes per launch / mean launch time.
-    # Per stage a pre-pass reads the stage state and writes its cell averages for both sweep
-    # orders (3*C*s per cell); each sweep reads its cell averages and writes a divergence
-    # (2*C*s), except the second sweep of stages 1-2, which reads its cell averages, the other
-    # divergence, u0 and the stage state and writes the stage result (5*C*s).
+    # Per stage a pre-pass reads the stage state and writes its cell averages (FP32: one
+    # order for both sweeps, 2*C*s per cell); each sweep reads the cell averages and writes a
+    # divergence (2*C*s), except the second sweep of stages 1-2, which reads the cell averages,
+    # the other divergence, u0 and the stage state and writes the stage result (5*C*s).
     # C = 4 stored variables, s = 4 bytes.
     C, sz = 4, 4
     alg_bytes_step = cells * C * sz * (2 + 2 + (2 + 5) + (2 + 5))
@@ -508,7 +508,7 @@ def main():
                 "alg_bytes_per_launch": alg_per_launch, "step_frac": step_alg * (value / ws) / cells / 1e9 / peak,
                 "note": "ALU/issue-bound stencil: thousands of FP32 ops per cell-update against 128 B"}
     if launches[3]:
-        ca_bytes = cells * C * sz * 3
+        ca_bytes = cells * C * sz * 2  # FP32: the state in, one order of cell averages out
         roofline["cell_average_prepass"] = {"launches": launches[3], "ms": kernel_ms[3],
                                             "achieved_gbs": ca_bytes / (kernel_ms[3] / launches[3] / 1e3) / 1e9,
                                             "alg_bytes_per_launch": ca_bytes}

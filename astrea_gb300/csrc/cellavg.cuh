@@ -19,8 +19,8 @@ namespace astrea {
 // One warp per strip of 30 columns x TY rows: its 32 lanes sit on 32
 // consecutive columns (lanes 0 and 31 are the strip's halo) and walk down the
 // rows, keeping rows i-1, i, i+1 (state and point primitives) in registers and
-// taking the axis-1 neighbours from the adjacent lanes; the next row's state is
-// loaded one row ahead.  No shared memory, no block barriers.
+// taking the axis-1 neighbours from the adjacent lanes; each row's state is
+// loaded two rows before it is converted.  No shared memory, no block barriers.
 constexpr int CA_W = 30, CA_NT = 256, CA_WARPS = CA_NT / 32;
 template <typename T, int MID> struct CellAvgTile {
   static constexpr int TY = 16;  // rows per strip
@@ -55,14 +55,20 @@ __global__ void __launch_bounds__(CA_NT) cell_average_kernel(const T* __restrict
 #pragma unroll
     for (int s = 0; s < NV; ++s) x[M::var(s)] = v[s];
   };
-  T qm[8], q0[8], qp[8], wm[8], w0[8], wp[8], nxt[NV];
+  T qm[8], q0[8], qp[8], wm[8], w0[8], wp[8], nxt[NV], nxt2[NV];  // nxt: row i+1, nxt2: row i+2
   {
     const T* pm = row_ptr(i0 - 1);
     const T* p0 = row_ptr(i0);
     const T* p1 = row_ptr(i0 + 1);
+    const T* p2 = row_ptr(i0 + 2);
     T a[NV], b[NV];
 #pragma unroll
-    for (int s = 0; s < NV; ++s) { a[s] = pm[s * plane]; b[s] = p0[s * plane]; nxt[s] = p1[s * plane]; }
+    for (int s = 0; s < NV; ++s) {
+      a[s] = pm[s * plane];
+      b[s] = p0[s * plane];
+      nxt[s] = p1[s * plane];
+      nxt2[s] = p2[s * plane];
+    }
     expand(a, qm);
     expand(b, q0);
     c2p<M>(qm, wm, gm1);
@@ -72,10 +78,12 @@ __global__ void __launch_bounds__(CA_NT) cell_average_kernel(const T* __restrict
     const int i = i0 + r;
     if (i >= n0) break;  // whole warp
     expand(nxt, qp);
-    if (r + 1 < TY) {  // the row after next, one row ahead of its use
-      const T* pn = row_ptr(i + 2);
 #pragma unroll
-      for (int s = 0; s < NV; ++s) nxt[s] = pn[s * plane];
+    for (int s = 0; s < NV; ++s) nxt[s] = nxt2[s];
+    if (r + 2 < TY) {  // row i+3, two rows ahead of its use
+      const T* pn = row_ptr(i + 3);
+#pragma unroll
+      for (int s = 0; s < NV; ++s) nxt2[s] = pn[s * plane];
     }
     c2p<M>(qp, wp, gm1);
     // axis-1 neighbours from the adjacent lanes

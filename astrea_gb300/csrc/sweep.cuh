@@ -278,6 +278,23 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 
   // element (gs, gt) of a grid-sized input, at a virtual index served by the boundary map
   auto gmap = [&](int v, int n) -> int { return (v >= 0 && v < n) ? v : bc_map(v, n, a.bc); };
+  // Stage combine (mode 1): the other divergence, u0 and the stage state of the tile's own
+  // cells are read only by the last level; their lines are requested from L2 now.  Each
+  // memory row of the tile is one segment of at most 128 bytes in FP32 (two lines at most),
+  // 256 bytes in FP64 (two lines, aligned): its first and last elements' lines cover it.
+  if constexpr (DIM == 2) {
+    if (a.mode == 1) {
+      constexpr int MR = AX == 1 ? TT : TS;  // memory rows of the tile (axis-0 indices)
+      const int seg = AX == 1 ? (s0 + TS <= Ns ? TS : Ns - s0) : (t0 + TT <= Nt ? TT : Nt - t0);
+      for (int e = tid; e < 3 * NV * MR * 2; e += nth) {
+        const int end = e & 1, r = (e >> 1) % MR, rest = (e >> 1) / MR, v = rest % NV, arr = rest / NV;
+        const int vs = AX == 1 ? s0 + end * (seg - 1) : s0 + r, vt = AX == 1 ? t0 + r : t0 + end * (seg - 1);
+        if (vs >= Ns || vt >= Nt) continue;
+        const T* base = arr == 0 ? a.dother : (arr == 1 ? a.u0 : a.q);
+        prefetch_l2(base + v * a.plane + gidx(vs, vt));
+      }
+    }
+  }
   // WSIN PPM tiles with viscosity: the viscous strip arrives by bulk copy (same for the whole CTA)
   bool strip_tma = false;
   T* qs_box = nullptr;

@@ -51,6 +51,11 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 }
 
 // 3D tiled bulk copy global -> shared (box origin x innermost); x * element size must be a multiple of 16
+// ask the L2 for the 128-byte line holding p (a hint: no data returns to the thread)
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
                                             unsigned long long* bar) {
   asm volatile(

@@ -38,13 +38,16 @@ template <typename T> struct BatchArgs {
   T* k1;
   T* d0;     // divergence arenas
   T* d1;
+  T* ws0;    // 2D: cell averages of the stage input for the axis-0 and axis-1 sweeps (the same arena in FP32)
+  T* ws1;
   int stage, mode, integ, want_emax, last_stage, dout_sel;
 };
 
+// 2D high-order combos stage the cell averages of a pre-pass (batched_cell_average_kernel)
 template <int MID, int DIM, int TS, int TT, typename T> constexpr size_t batch_smem_elems() {
   constexpr int NV = Model<MID>::NV;
-  constexpr int a = Smem<PLM, DIM, TS, TT, NV>::total, b = Smem<PPM, DIM, TS, TT, NV>::total,
-                c = Smem<WENO5, DIM, TS, TT, NV>::total;
+  constexpr int a = Smem<PLM, DIM, TS, TT, NV>::total, b = Smem<PPM, DIM, TS, TT, NV, DIM == 2>::total,
+                c = Smem<WENO5, DIM, TS, TT, NV, DIM == 2>::total;
   constexpr int m = a > b ? a : b;
   return (size_t)(m > c ? m : c);
 }
@@ -88,13 +91,15 @@ __global__ void __launch_bounds__((NT > 256 ? NT : 256), (SweepOcc<T, MID, (NT >
     a.u0 = b.u + gd.base;
     a.out = out + gd.base;
     a.clock = clk;
+    constexpr bool WS = DIM == 2;  // PPM / WENO5 tiles stage the pre-pass's cell averages
+    if (WS) a.ws = (AX == 0 ? b.ws0 : b.ws1) + gd.base;
     switch (gd.combo) {
       case C_PLM_LLF: sweep_tile<T, MID, PLM, LLF, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
       case C_PLM_HLL: sweep_tile<T, MID, PLM, HLL, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
-      case C_PPM_LLF: sweep_tile<T, MID, PPM, LLF, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
-      case C_PPM_HLL: sweep_tile<T, MID, PPM, HLL, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
-      case C_WENO5_LLF: sweep_tile<T, MID, WENO5, LLF, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
-      default: sweep_tile<T, MID, WENO5, HLL, DIM, AX, TS, TT, NT>(a, w.s0, w.t0, smem_raw); break;
+      case C_PPM_LLF: sweep_tile<T, MID, PPM, LLF, DIM, AX, TS, TT, NT, false, WS>(a, w.s0, w.t0, smem_raw); break;
+      case C_PPM_HLL: sweep_tile<T, MID, PPM, HLL, DIM, AX, TS, TT, NT, false, WS>(a, w.s0, w.t0, smem_raw); break;
+      case C_WENO5_LLF: sweep_tile<T, MID, WENO5, LLF, DIM, AX, TS, TT, NT, false, WS>(a, w.s0, w.t0, smem_raw); break;
+      default: sweep_tile<T, MID, WENO5, HLL, DIM, AX, TS, TT, NT, false, WS>(a, w.s0, w.t0, smem_raw); break;
     }
   }
 }

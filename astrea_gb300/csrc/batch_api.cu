@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "batch_launch.cuh"
+#include "cellavg.cuh"
 #include "host_common.h"
 
 using namespace astrea;
@@ -95,6 +96,12 @@ struct astrea_batch {
 
 template <typename T> struct Batch final : IBatch {
   T *k0 = nullptr, *k1 = nullptr, *d0 = nullptr, *d1 = nullptr, *tmp = nullptr;
+  // 2D: cell averages of each stage input for the high-order grids (FP64: one arena per sweep order)
+  T *ws0 = nullptr, *ws1 = nullptr;
+  BatchedCellAvgFn<T> cavg = nullptr;
+  BStrip* strips = nullptr;
+  size_t strips_cap = 0;
+  int nstrips = 0;
   BGrid<T>* d_grids = nullptr;
   BatchFn<T> cand[2][NBTILES2] = {};  // tile candidates per axis (nullptr: not built)
   int occ_c[2][NBTILES2] = {};
@@ -103,6 +110,9 @@ template <typename T> struct Batch final : IBatch {
 
   ~Batch() override {
     cudaFree(k0); cudaFree(k1); cudaFree(d0); cudaFree(d1); cudaFree(tmp); cudaFree(d_grids);
+    cudaFree(ws0);
+    if (ws1 != ws0) cudaFree(ws1);
+    cudaFree(strips);
   }
 
   int alloc() override {
@@ -111,6 +121,16 @@ template <typename T> struct Batch final : IBatch {
         cudaMalloc(&d0, bytes) != cudaSuccess || cudaMalloc(&d1, bytes) != cudaSuccess ||
         cudaMalloc(&tmp, bytes) != cudaSuccess)
       return fail(ASTREA_ERR_OOM, "batch stage buffers allocation failed");
+    if (dim == 2) {
+      if (cudaMalloc(&ws0, bytes) != cudaSuccess) return fail(ASTREA_ERR_OOM, "batch cell-average arena allocation failed");
+      ws1 = ws0;
+      if (cell_average_both_orders<T>() && cudaMalloc(&ws1, bytes) != cudaSuccess) {
+        ws1 = nullptr;
+        return fail(ASTREA_ERR_OOM, "batch cell-average arena allocation failed");
+      }
+      cavg = get_batched_cell_average<T>(model);
+      if (!cavg) return fail(ASTREA_ERR_CONFIG, "no batched cell-average kernel for this model");
+    }
     CK(cudaMalloc(&d_grids, sizeof(BGrid<T>) * max_slots));
     CK(cudaMalloc(&counters, sizeof(int) * 16));
     int dev = 0;
@@ -158,6 +178,8 @@ template <typename T> struct Batch final : IBatch {
         b.mode = 0;
         b.want_emax = 0;
         b.dout_sel = ax;
+        rc = launch_cell_average(b, st);
+        if (rc) return rc;
         rc = launch_sweep(b, ax, 15, st);
         if (rc) return rc;
         CK(cudaEventRecord(e0, st));
@@ -222,7 +244,35 @@ template <typename T> struct Batch final : IBatch {
       if (!it.empty()) CK(cudaMemcpy(items[ax], it.data(), sizeof(BItem) * it.size(), cudaMemcpyHostToDevice));
       nctas[ax] = std::max(1, std::min(nitems[ax], occ_c[ax][var[ax]] * sms));
     }
+    // cell-average strips of the 2D high-order grids: 30 columns x TY rows each
+    nstrips = 0;
+    if (dim == 2) {
+      constexpr int TY = CellAvgTile<T, 4>::TY;
+      static_assert(CellAvgTile<T, 4>::TY == CellAvgTile<T, 8>::TY, "one strip height per precision");
+      std::vector<BStrip> sl;
+      for (int g : order) {
+        const astrea_grid& a = host_grids[g];
+        if (a.scheme < PPM) continue;
+        for (int i0 = 0; i0 < a.n0; i0 += TY)
+          for (int j0 = 0; j0 < a.n1; j0 += CA_W) sl.push_back(BStrip{g, i0, j0 - 1});
+      }
+      nstrips = (int)sl.size();
+      if (sl.size() > strips_cap) {
+        cudaFree(strips);
+        strips = nullptr;
+        strips_cap = std::max<size_t>(sl.size(), 2 * strips_cap);
+        CK(cudaMalloc(&strips, sizeof(BStrip) * strips_cap));
+      }
+      if (!sl.empty()) CK(cudaMemcpy(strips, sl.data(), sizeof(BStrip) * sl.size(), cudaMemcpyHostToDevice));
+    }
     dirty = false;
+    return ASTREA_OK;
+  }
+
+  // the cell averages of this stage's input for every 2D high-order grid
+  int launch_cell_average(const BatchArgs<T>& b, cudaStream_t st) {
+    if (!cavg || nstrips == 0) return ASTREA_OK;
+    CK(cavg(b, strips, nstrips, st));
     return ASTREA_OK;
   }
 
@@ -235,6 +285,8 @@ template <typename T> struct Batch final : IBatch {
     b.k1 = k1;
     b.d0 = d0;
     b.d1 = d1;
+    b.ws0 = ws0;
+    b.ws1 = ws1;
     b.integ = integrator;
     return b;
   }
@@ -261,6 +313,8 @@ template <typename T> struct Batch final : IBatch {
     b.stage = 0;
     b.mode = 0;
     b.want_emax = 1;
+    int prc = launch_cell_average(b, st);
+    if (prc) return prc;
     for (int ax = 0; ax < dim; ++ax) {
       b.dout_sel = ax;
       int rc = launch_sweep(b, ax, slot++, st);
@@ -278,9 +332,11 @@ template <typename T> struct Batch final : IBatch {
       c.stage = s;
       c.last_stage = s == ns - 1;
       if (dim == 2) {
+        int rc = launch_cell_average(c, st);
+        if (rc) return rc;
         c.mode = 0;
         c.dout_sel = 0;
-        int rc = launch_sweep(c, 0, slot++, st);
+        rc = launch_sweep(c, 0, slot++, st);
         if (rc) return rc;
         c.mode = 1;
         rc = launch_sweep(c, 1, slot++, st);

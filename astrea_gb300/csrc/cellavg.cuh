@@ -12,7 +12,7 @@
 // periodic), the values the sweep tiles' own q level holds there.  The
 // arithmetic is the sweep's, operation for operation.
 #pragma once
-#include "sweep.cuh"
+#include "batch.cuh"
 
 namespace astrea {
 
@@ -31,18 +31,17 @@ template <typename T, int MID> struct CellAvgTile {
 // from the other order's in the last FP32 bit).
 template <typename T> constexpr bool cell_average_both_orders() { return Prec<T>::EXACT; }
 
+// One strip, rows [i0, i0+TY) and the 30 columns after jb, by one whole warp
+// (every lane reaches every shuffle).
 template <typename T, int MID>
-__global__ void __launch_bounds__(CA_NT) cell_average_kernel(const T* __restrict__ q, T* __restrict__ w_ax0,
-                                                             T* __restrict__ w_ax1, int n0, int n1, long long plane,
-                                                             int bc, T gm1, const Clock* clk) {
-  if (clk->done) return;
+__device__ __forceinline__ void cell_average_strip(const T* __restrict__ q, T* __restrict__ w_ax0,
+                                                   T* __restrict__ w_ax1, int n0, int n1, long long plane, int bc,
+                                                   T gm1, int i0, int jb) {
   using M = Model<MID>;
   constexpr int NV = M::NV, TY = CellAvgTile<T, MID>::TY;
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int i0 = (blockIdx.y * CA_WARPS + (threadIdx.x >> 5)) * TY;
-  if (i0 >= n0) return;  // whole warp
-  const int j = blockIdx.x * CA_W - 1 + lane;
+  const int j = jb + lane;
   const int gj = (j >= 0 && j < n1) ? j : bc_map(j, n1, bc);
   const bool out_lane = lane >= 1 && lane <= CA_W && j < n1;
   auto row_ptr = [&](int i) -> const T* {
@@ -145,6 +144,34 @@ __global__ void __launch_bounds__(CA_NT) cell_average_kernel(const T* __restrict
   }
 }
 
+template <typename T, int MID>
+__global__ void __launch_bounds__(CA_NT) cell_average_kernel(const T* __restrict__ q, T* __restrict__ w_ax0,
+                                                             T* __restrict__ w_ax1, int n0, int n1, long long plane,
+                                                             int bc, T gm1, const Clock* clk) {
+  if (clk->done) return;
+  const int i0 = (blockIdx.y * CA_WARPS + (threadIdx.x >> 5)) * CellAvgTile<T, MID>::TY;
+  if (i0 >= n0) return;  // whole warp
+  cell_average_strip<T, MID>(q, w_ax0, w_ax1, n0, n1, plane, bc, gm1, i0, blockIdx.x * CA_W - 1);
+}
+
+// Batched form: one warp per strip of a list over the high-order grids of a batch
+// (the stage input and the cell averages at each grid's arena offset).
+struct BStrip {
+  int g, i0, jb;
+};
+template <typename T, int MID>
+__global__ void __launch_bounds__(CA_NT) batched_cell_average_kernel(const BatchArgs<T> b, const BStrip* __restrict__ strips,
+                                                                     int nstrips) {
+  const int it = blockIdx.x * CA_WARPS + (threadIdx.x >> 5);
+  if (it >= nstrips) return;  // whole warp
+  const BStrip w = strips[it];
+  if (b.clocks[w.g].done) return;
+  const BGrid<T>& gd = b.grids[w.g];
+  const T* cur = b.stage == 0 ? b.u : ((b.stage - 1) % 2 == 0 ? b.k0 : b.k1);
+  cell_average_strip<T, MID>(cur + gd.base, b.ws0 + gd.base, b.ws1 + gd.base, gd.n0, gd.n1, gd.cells, gd.bc, gd.gm1,
+                             w.i0, w.jb);
+}
+
 template <typename T> using CellAvgFn = cudaError_t (*)(const T* q, T* w_ax0, T* w_ax1, int n0, int n1,
                                                         long long plane, int bc, T gm1, const Clock* clk,
                                                         cudaStream_t st);
@@ -158,6 +185,15 @@ cudaError_t launch_cell_average(const T* q, T* w_ax0, T* w_ax1, int n0, int n1, 
   return cudaGetLastError();
 }
 
+template <typename T> using BatchedCellAvgFn = cudaError_t (*)(const BatchArgs<T>&, const BStrip*, int, cudaStream_t);
+
+template <typename T, int MID>
+cudaError_t launch_batched_cell_average(const BatchArgs<T>& b, const BStrip* strips, int nstrips, cudaStream_t st) {
+  if (nstrips <= 0) return cudaSuccess;
+  batched_cell_average_kernel<T, MID><<<(nstrips + CA_WARPS - 1) / CA_WARPS, CA_NT, 0, st>>>(b, strips, nstrips);
+  return cudaGetLastError();
+}
+
 // the launcher of a 2D model (4: Euler, 8: MHD / transverse velocities); nullptr otherwise.
 // Instantiated in cellavg_f32.cu (FMA, like the FP32 sweeps) and cellavg_f64.cu
 // (no FMA, like the FP64 sweeps).
@@ -167,7 +203,15 @@ template <typename T> CellAvgFn<T> get_cell_average(int model) {
   return nullptr;
 }
 
+template <typename T> BatchedCellAvgFn<T> get_batched_cell_average(int model) {
+  if (model == 4) return &launch_batched_cell_average<T, 4>;
+  if (model == 8) return &launch_batched_cell_average<T, 8>;
+  return nullptr;
+}
+
 extern template CellAvgFn<float> get_cell_average<float>(int);
 extern template CellAvgFn<double> get_cell_average<double>(int);
+extern template BatchedCellAvgFn<float> get_batched_cell_average<float>(int);
+extern template BatchedCellAvgFn<double> get_batched_cell_average<double>(int);
 
 }  // namespace astrea

@@ -2,4 +2,5 @@
 #include "cellavg.cuh"
 namespace astrea {
 template CellAvgFn<float> get_cell_average<float>(int);
+template BatchedCellAvgFn<float> get_batched_cell_average<float>(int);
 }

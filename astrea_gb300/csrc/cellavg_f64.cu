@@ -2,4 +2,5 @@
 #include "cellavg.cuh"
 namespace astrea {
 template CellAvgFn<double> get_cell_average<double>(int);
+template BatchedCellAvgFn<double> get_batched_cell_average<double>(int);
 }

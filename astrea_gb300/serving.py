@@ -27,9 +27,14 @@ import torch
 from .batch import SlotBatch
 from .solver import RunConfig
 
-# bytes of device memory one state element costs in a class: the caller-side state
-# and primitive arenas plus the engine's two stage and two divergence buffers and one scratch
+# arenas of the state's size a class holds: the caller-side state and primitive arenas
+# plus the engine's two stage, two divergence and one scratch arena, and in 2D the cell
+# averages of the high-order schemes (one arena in FP32, one per sweep order in FP64)
 ARENA_COPIES = 7
+
+
+def arena_copies(dim, precision):
+    return ARENA_COPIES + (0 if dim == 1 else (1 if precision == 32 else 2))
 
 
 @dataclass
@@ -193,7 +198,7 @@ class Server:
         self.batches, self.arenas, self.streams, self.free_slots = {}, {}, {}, {}
         self.classes = []
         for cls in self.CLASSES:
-            cap = int(hbm_budget_bytes * shares.get(cls, 0) / (ARENA_COPIES * esize))
+            cap = int(hbm_budget_bytes * shares.get(cls, 0) / (arena_copies(cls[0], precision) * esize))
             cap -= cap % 8
             if cap <= 0:
                 continue

@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 import torch
 
-from astrea_gb300.serving import Server, make_requests
+from astrea_gb300.serving import Server, arena_copies, make_requests
 from astrea_gb300.solver import Solver
 
 pytestmark = pytest.mark.gpu
@@ -51,7 +51,8 @@ def test_mix_equals_alone():
 def test_admission_respects_the_memory_budget():
     reqs = make_requests(6, rate=1e6, seed=12, n1d=(64, 128), n2d=(128, 128), frac_1d=0.0, frac_mhd=0.0,
                          t_end=(0.01, 0.02))
-    srv = Server(hbm_budget_bytes=7 * 4 * 4 * 128 * 128 * 2 / 0.5, precision=32, max_slots=8,
+    # room for exactly two 128^2 Euler grids in the (2, 4) class
+    srv = Server(hbm_budget_bytes=arena_copies(2, 32) * 4 * 4 * 128 * 128 * 2 / 0.5, precision=32, max_slots=8,
                  shares={(1, 3): 0, (1, 8): 0, (2, 4): .5, (2, 8): .5}, steps_per_poll=1)
     stats = srv.serve(reqs, realtime=False)
     assert len(stats.latencies_ms) == len(reqs)

@@ -58,6 +58,27 @@ int stages_count(int integ) {
 
 }  // namespace
 
+// Slot changes (occupy, release) are queued on the host and applied on the
+// device by the next step, stream-ordered, so that admitting or retiring a grid
+// never synchronises the device.  The changes travel as kernel parameters.
+template <typename T> struct SlotUpdate {
+  int slot, has_grid;
+  BGrid<T> grid;
+  Clock clock;
+};
+constexpr int kUpdatesPerLaunch = 16;
+template <typename T> struct SlotUpdates {
+  SlotUpdate<T> u[kUpdatesPerLaunch];
+  int n;
+};
+static_assert(sizeof(SlotUpdates<double>) <= 4000, "slot updates exceed the kernel parameter space");
+template <typename T> __global__ void apply_slot_updates(const SlotUpdates<T> up, BGrid<T>* grids, Clock* clocks) {
+  const int i = threadIdx.x;
+  if (i >= up.n) return;
+  if (up.u[i].has_grid) grids[up.u[i].slot] = up.u[i].grid;
+  clocks[up.u[i].slot] = up.u[i].clock;
+}
+
 struct IBatch {
   int dim = 2, model = 4, precision = 32, integrator = SSPRK33, max_slots = 0, nv = 0;
   long long capacity = 0;  // elements per arena
@@ -80,8 +101,13 @@ struct IBatch {
     cudaFree(items[1]);
   }
   virtual int alloc() = 0;
-  virtual int set_slot(int slot, const astrea_grid& g, long long offset) = 0;
-  virtual int rebuild() = 0;
+  // queue the grid of a slot and its initial clock (applied by the next step)
+  virtual int set_slot(int slot, const astrea_grid& g, long long offset, const Clock& c) = 0;
+  // queue a slot's release: its clock reads done, so every kernel skips it
+  virtual void clear_slot(int slot) = 0;
+  // apply the queued slot changes on ``st``
+  virtual int flush(cudaStream_t st) = 0;
+  virtual int rebuild(cudaStream_t st) = 0;
   virtual int enqueue_step(void* arena, cudaStream_t st) = 0;
   virtual int initialise(int slot, const void* prim, void* arena, cudaStream_t st) = 0;
   // pick each axis's tile (once, at the first step with occupied slots; not during a capture)
@@ -103,6 +129,13 @@ template <typename T> struct Batch final : IBatch {
   size_t strips_cap = 0;
   int nstrips = 0;
   BGrid<T>* d_grids = nullptr;
+  std::vector<SlotUpdate<T>> pending;  // at most one per slot, in queue order
+  // pinned staging of the work lists, two used in turn; each is rewritten only after
+  // the copies that read it last have run (its event)
+  char* stage_h[2] = {nullptr, nullptr};
+  size_t stage_cap[2] = {0, 0};
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  int stage_i = 0;
   BatchFn<T> cand[2][NBTILES2] = {};  // tile candidates per axis (nullptr: not built)
   int occ_c[2][NBTILES2] = {};
   int nctas[2] = {0, 0};
@@ -113,6 +146,10 @@ template <typename T> struct Batch final : IBatch {
     cudaFree(ws0);
     if (ws1 != ws0) cudaFree(ws1);
     cudaFree(strips);
+    for (int i = 0; i < 2; ++i) {
+      if (stage_ev[i]) cudaEventDestroy(stage_ev[i]);
+      cudaFreeHost(stage_h[i]);
+    }
   }
 
   int alloc() override {
@@ -171,7 +208,7 @@ template <typename T> struct Batch final : IBatch {
       for (int v = 0; v < NBTILES2; ++v) {
         if (!cand[ax][v]) continue;
         var[ax] = v;
-        int rc = rebuild();
+        int rc = rebuild(st);
         if (rc) return rc;
         BatchArgs<T> b = args(static_cast<T*>(arena));
         b.stage = 0;
@@ -201,7 +238,7 @@ template <typename T> struct Batch final : IBatch {
     return ASTREA_OK;
   }
 
-  int set_slot(int slot, const astrea_grid& a, long long offset) override {
+  int set_slot(int slot, const astrea_grid& a, long long offset, const Clock& c) override {
     BGrid<T> d{};
     d.base = offset;
     d.cells = (long long)a.n0 * (dim == 2 ? a.n1 : 1);
@@ -214,34 +251,63 @@ template <typename T> struct Batch final : IBatch {
     d.gamma = T(a.gamma);
     d.gm1 = T(a.gamma - 1.0);
     d.dx = a.dx;
-    CK(cudaMemcpy(d_grids + slot, &d, sizeof(d), cudaMemcpyHostToDevice));
+    queue(SlotUpdate<T>{slot, 1, d, c});
     return ASTREA_OK;
   }
 
-  int rebuild() override {
+  void queue(const SlotUpdate<T>& u) {
+    for (auto& p : pending)
+      if (p.slot == u.slot) {
+        if (u.has_grid) { p.has_grid = 1; p.grid = u.grid; }
+        p.clock = u.clock;
+        return;
+      }
+    pending.push_back(u);
+  }
+
+  void clear_slot(int slot) override {
+    SlotUpdate<T> u{};
+    u.slot = slot;
+    u.has_grid = 0;
+    u.clock.done = 1;
+    queue(u);
+  }
+
+  int flush(cudaStream_t st) override {
+    for (size_t i = 0; i < pending.size(); i += kUpdatesPerLaunch) {
+      SlotUpdates<T> up{};
+      up.n = (int)std::min<size_t>(kUpdatesPerLaunch, pending.size() - i);
+      for (int k = 0; k < up.n; ++k) up.u[k] = pending[i + k];
+      apply_slot_updates<T><<<1, kUpdatesPerLaunch, 0, st>>>(up, d_grids, clocks);
+      CK(cudaGetLastError());
+    }
+    pending.clear();
+    return ASTREA_OK;
+  }
+
+  int rebuild(cudaStream_t st) override {
     std::vector<int> order;
     for (int s = 0; s < max_slots; ++s)
       if (active[s]) order.push_back(s);
     auto cells = [&](int s) { return (long long)host_grids[s].n0 * (dim == 2 ? host_grids[s].n1 : 1); };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cells(x) > cells(y); });
+    std::vector<BItem> it[2];
     for (int ax = 0; ax < dim; ++ax) {
       const int TS = tile_ts(dim, var[ax]), TT = tile_tt(dim, var[ax]);
-      std::vector<BItem> it;
       for (int g : order) {
         const astrea_grid& a = host_grids[g];
         const int Ns = dim == 1 ? a.n0 : (ax == 0 ? a.n0 : a.n1);
         const int Nt = dim == 1 ? 1 : (ax == 0 ? a.n1 : a.n0);
         for (int s0 = 0; s0 < Ns; s0 += TS)
-          for (int t0 = 0; t0 < Nt; t0 += TT) it.push_back(BItem{g, s0, t0});
+          for (int t0 = 0; t0 < Nt; t0 += TT) it[ax].push_back(BItem{g, s0, t0});
       }
-      nitems[ax] = (int)it.size();
-      if (it.size() > items_cap[ax]) {
-        cudaFree(items[ax]);
+      nitems[ax] = (int)it[ax].size();
+      if (it[ax].size() > items_cap[ax]) {
+        cudaFree(items[ax]);  // (synchronises the device; the lists only grow geometrically)
         items[ax] = nullptr;
-        items_cap[ax] = std::max<size_t>(it.size(), 2 * items_cap[ax]);
+        items_cap[ax] = std::max<size_t>(it[ax].size(), 2 * items_cap[ax]);
         CK(cudaMalloc(&items[ax], sizeof(BItem) * items_cap[ax]));
       }
-      if (!it.empty()) CK(cudaMemcpy(items[ax], it.data(), sizeof(BItem) * it.size(), cudaMemcpyHostToDevice));
       nctas[ax] = std::max(1, std::min(nitems[ax], occ_c[ax][var[ax]] * sms));
     }
     // cell-average strips of the 2D high-order grids: 30 columns x TY rows each
@@ -263,9 +329,37 @@ template <typename T> struct Batch final : IBatch {
         strips_cap = std::max<size_t>(sl.size(), 2 * strips_cap);
         CK(cudaMalloc(&strips, sizeof(BStrip) * strips_cap));
       }
-      if (!sl.empty()) CK(cudaMemcpy(strips, sl.data(), sizeof(BStrip) * sl.size(), cudaMemcpyHostToDevice));
+      stage_lists(it, sl, st);
+    } else {
+      stage_lists(it, std::vector<BStrip>(), st);
     }
     dirty = false;
+    return ASTREA_OK;
+  }
+
+  // upload the work lists on ``st`` through a pinned staging buffer (no device synchronisation)
+  int stage_lists(const std::vector<BItem>* it, const std::vector<BStrip>& sl, cudaStream_t st) {
+    const size_t b0 = sizeof(BItem) * it[0].size(), b1 = sizeof(BItem) * it[1].size(), b2 = sizeof(BStrip) * sl.size();
+    const size_t need = b0 + b1 + b2;
+    if (need == 0) return ASTREA_OK;
+    const int k = stage_i;
+    stage_i ^= 1;
+    if (!stage_ev[k]) CK(cudaEventCreateWithFlags(&stage_ev[k], cudaEventDisableTiming));
+    else CK(cudaEventSynchronize(stage_ev[k]));  // the copies that last read this buffer have run
+    if (need > stage_cap[k]) {
+      cudaFreeHost(stage_h[k]);
+      stage_h[k] = nullptr;
+      stage_cap[k] = std::max(need, 2 * stage_cap[k]);
+      CK(cudaMallocHost(reinterpret_cast<void**>(&stage_h[k]), stage_cap[k]));
+    }
+    char* h = stage_h[k];
+    if (b0) std::memcpy(h, it[0].data(), b0);
+    if (b1) std::memcpy(h + b0, it[1].data(), b1);
+    if (b2) std::memcpy(h + b0 + b1, sl.data(), b2);
+    if (b0) CK(cudaMemcpyAsync(items[0], h, b0, cudaMemcpyHostToDevice, st));
+    if (b1) CK(cudaMemcpyAsync(items[1], h + b0, b1, cudaMemcpyHostToDevice, st));
+    if (b2) CK(cudaMemcpyAsync(strips, h + b0 + b1, b2, cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(stage_ev[k], st));
     return ASTREA_OK;
   }
 
@@ -302,8 +396,10 @@ template <typename T> struct Batch final : IBatch {
   }
 
   int enqueue_step(void* arena, cudaStream_t st) override {
+    int frc = flush(st);  // (nothing is queued inside a graph capture: the caller flushed before it)
+    if (frc) return frc;
     if (dirty) {
-      int rc = rebuild();
+      int rc = rebuild(st);
       if (rc) return rc;
     }
     T* u = static_cast<T*>(arena);
@@ -432,10 +528,6 @@ int astrea_batch_set(astrea_batch* h, int slot, const astrea_grid* grid, long lo
   if (rc) return rc;
   const long long need = (long long)b->nv * grid->n0 * (b->dim == 2 ? grid->n1 : 1);
   if (offset < 0 || offset + need > b->capacity) return fail(ASTREA_ERR_OOM, "grid does not fit in the batch arena");
-  b->host_grids[slot] = *grid;
-  b->offsets[slot] = offset;
-  rc = b->set_slot(slot, *grid, offset);
-  if (rc) return rc;
   Clock c;
   std::memset(&c, 0, sizeof(c));
   c.t_end = grid->t_end;
@@ -445,7 +537,10 @@ int astrea_batch_set(astrea_batch* h, int slot, const astrea_grid* grid, long lo
   c.idx = 1;
   c.naxes = b->dim;
   c.done = !(0.0 < grid->t_end);
-  CK(cudaMemcpy(b->clocks + slot, &c, sizeof(c), cudaMemcpyHostToDevice));
+  rc = b->set_slot(slot, *grid, offset, c);  // applied on the device by the next step (or clock read)
+  if (rc) return rc;
+  b->host_grids[slot] = *grid;
+  b->offsets[slot] = offset;
   b->active[slot] = 1;
   b->dirty = true;
   return ASTREA_OK;
@@ -455,8 +550,7 @@ int astrea_batch_clear(astrea_batch* h, int slot) {
   if (!h) return fail(ASTREA_ERR_ARG, "NULL argument");
   IBatch* b = h->b;
   if (slot < 0 || slot >= b->max_slots) return fail(ASTREA_ERR_ARG, "slot out of range");
-  int one = 1;
-  CK(cudaMemcpy(&b->clocks[slot].done, &one, sizeof(int), cudaMemcpyHostToDevice));
+  b->clear_slot(slot);  // applied on the device by the next step (or clock read)
   b->active[slot] = 0;
   b->dirty = true;
   return ASTREA_OK;
@@ -477,6 +571,8 @@ int astrea_batch_tile(const astrea_batch* h, int axis, int* ts, int* tt) {
 
 int astrea_batch_step(astrea_batch* h, void* arena, int nsteps, void* stream) {
   if (!h || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
+  int frc = h->b->flush(static_cast<cudaStream_t>(stream));
+  if (frc) return frc;
   int trc = h->b->tune(arena, static_cast<cudaStream_t>(stream));
   if (trc) return trc;
   for (int i = 0; i < nsteps; ++i) {
@@ -490,6 +586,8 @@ int astrea_batch_graph_step(astrea_batch* h, void* arena, int nsteps, void* stre
   if (!h || !arena) return fail(ASTREA_ERR_ARG, "NULL argument");
   IBatch* b = h->b;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int frc = b->flush(st);  // before any capture: the captured step has nothing queued
+  if (frc) return frc;
   int trc = b->tune(arena, st);
   if (trc) return trc;
   if (b->dirty || !b->graph || b->graph_arena != arena) {
@@ -498,7 +596,7 @@ int astrea_batch_graph_step(astrea_batch* h, void* arena, int nsteps, void* stre
       b->graph = nullptr;
     }
     if (b->dirty) {
-      int rc = b->rebuild();
+      int rc = b->rebuild(st);
       if (rc) return rc;
     }
     cudaStream_t cap;
@@ -524,6 +622,8 @@ int astrea_batch_clocks(astrea_batch* h, double* t, double* dt, int* steps, int*
   IBatch* b = h->b;
   std::vector<Clock> c(b->max_slots);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int frc = b->flush(st);  // queued slot changes first
+  if (frc) return frc;
   CK(cudaMemcpyAsync(c.data(), b->clocks, sizeof(Clock) * b->max_slots, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   for (int g = 0; g < b->max_slots; ++g) {

@@ -164,6 +164,19 @@ class Arena:
         self.free = merged
 
 
+def stalled(steps, t, dt, t_end, max_steps, check_after=1000):
+    """Whether a running request is retired for its time step: past ``max_steps`` steps, or, once it has
+    taken ``check_after`` steps, when its current dt would need more than ``max_steps`` steps in all to
+    reach ``t_end`` (a step that collapsed on near-vacuum states does not recover in time)."""
+    if max_steps is None:
+        return False
+    if steps > max_steps:
+        return True
+    if steps < check_after:
+        return False
+    return not (dt > 0) or (t_end - t) / dt > max_steps - steps
+
+
 @dataclass
 class ServeStats:
     latencies_ms: list = field(default_factory=list)
@@ -190,7 +203,8 @@ class Server:
                  steps_per_poll=4, device=None, max_steps=None):
         self.precision = precision
         # a request whose time step collapsed (near-vacuum states with finite speeds) would never reach its
-        # end time; past ``max_steps`` steps it is retired with status bit 2
+        # end time; once it is past, or projected past, ``max_steps`` steps it is retired with status bit 2
+        # (value 4; see ``stalled``)
         self.max_steps = max_steps
         esize = 4 if precision == 32 else 8
         shares = shares or {(1, 3): .1, (1, 8): .1, (2, 4): .5, (2, 8): .3}
@@ -268,7 +282,9 @@ class Server:
                     clk = self.batches[cls].clocks()
                 now = time.perf_counter() - t0
                 for slot in list(self.active[cls].keys()):
-                    over = self.max_steps is not None and clk["steps"][slot] > self.max_steps
+                    r = self.active[cls][slot][0]
+                    over = not clk["done"][slot] and stalled(int(clk["steps"][slot]), float(clk["t"][slot]),
+                                                             float(clk["dt"][slot]), r.t_end, self.max_steps)
                     if not clk["done"][slot] and not over:
                         continue
                     r, off, size = self.active[cls].pop(slot)

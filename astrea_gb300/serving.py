@@ -200,7 +200,7 @@ class Server:
     CLASSES = ((1, 3), (1, 8), (2, 4), (2, 8))
 
     def __init__(self, hbm_budget_bytes=150e9, precision=32, max_slots=256, shares=None, keep_results=False,
-                 steps_per_poll=4, device=None, max_steps=None):
+                 steps_per_poll=4, device=None, max_steps=None, max_steps_per_poll=32, graph=True):
         self.precision = precision
         # a request whose time step collapsed (near-vacuum states with finite speeds) would never reach its
         # end time; once it is past, or projected past, ``max_steps`` steps it is retired with status bit 2
@@ -222,7 +222,13 @@ class Server:
             self.streams[cls] = torch.cuda.Stream(self.device)
             self.free_slots[cls] = list(range(max_slots))[::-1]
         self.keep_results = keep_results
+        # steps per poll of a class: ``steps_per_poll`` while it has requests without a clock reading yet,
+        # else the fewest steps any of its requests still needs (at least 1, at most ``max_steps_per_poll``),
+        # so that polls land on completions; every poll's steps replay one captured CUDA graph
         self.steps_per_poll = steps_per_poll
+        self.max_steps_per_poll = max_steps_per_poll
+        self.graph = graph
+        self.last_clk = {}
 
     def _admit(self, r, now):
         cls = (r.dim, r.model)
@@ -240,6 +246,20 @@ class Server:
         self.active[cls][slot] = (r, off, size)
         return True
 
+    def _poll_steps(self, cls):
+        last = self.last_clk.get(cls)
+        if last is None or any(last[1].get(slot) != e[0].rid for slot, e in self.active[cls].items()):
+            return self.steps_per_poll
+        clk = last[0]
+        need = self.max_steps_per_poll
+        for slot, (r, _, _) in self.active[cls].items():
+            dt = float(clk["dt"][slot])
+            if dt > 0 and math.isfinite(dt):
+                need = min(need, math.ceil((r.t_end - float(clk["t"][slot])) / dt))
+            else:
+                need = 1
+        return max(1, min(need, self.max_steps_per_poll))
+
     def serve(self, requests, realtime=True, max_wall_s=None):
         """Run the request stream; returns ServeStats (requests are updated in place)."""
         stats = ServeStats()
@@ -253,6 +273,7 @@ class Server:
                 raise ValueError(f"request {r.rid} ({size} elements) exceeds its class arena")
             pending[cls].append(r)
         self.active = {cls: {} for cls in self.classes}
+        self.last_clk = {}
         t0 = time.perf_counter()
         while any(pending.values()) or any(self.active.values()):
             now = time.perf_counter() - t0
@@ -274,12 +295,13 @@ class Server:
             for cls in self.classes:
                 if self.active[cls]:
                     with torch.cuda.stream(self.streams[cls]):
-                        self.batches[cls].step(self.steps_per_poll)
+                        self.batches[cls].step(self._poll_steps(cls), graph=self.graph)
             for cls in self.classes:
                 if not self.active[cls]:
                     continue
                 with torch.cuda.stream(self.streams[cls]):
                     clk = self.batches[cls].clocks()
+                self.last_clk[cls] = (clk, {slot: e[0].rid for slot, e in self.active[cls].items()})
                 now = time.perf_counter() - t0
                 for slot in list(self.active[cls].keys()):
                     r = self.active[cls][slot][0]

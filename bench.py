@@ -52,6 +52,15 @@ WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc) with flattening and ar
 # the stage state once more besides its cell averages.
 SWEEP_DRAM_BYTES = 218.6e6
 SWEEP_DRAM_CELLS = 2048 * 2048
+# Floating-point operations per cell-update of one SSPRK3 step (every kernel of the step),
+# from ncu's SASS op counters (fadd + fmul + 2 x ffma, and the FP64 counterparts) over one
+# step of the workload at 512^2 (profiles/flops_step_2d_shear.md).  FP64 division and square
+# root are instruction sequences, which is why the FP64 step counts more operations.
+FLOPS_FP32_PER_CELL_UPDATE = 5005.1
+FLOPS_FP64_PER_CELL_UPDATE = 11979.3
+# per-SM, per-clock issue rates of the FP32 and FP64 fused multiply-add pipes on GB300
+# (ncu: sm__sass_thread_inst_executed_op_{ffma,dfma}_pred_on.sum.peak_sustained / SMs)
+FFMA_PER_SM_CLK, DFMA_PER_SM_CLK = 128, 2
 
 
 def shear_layer(n, seed=SEED):
@@ -132,6 +141,24 @@ class ClockSampler:
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def alu_roofline(value32, value64, sm_max_mhz):
+    """FP32 and FP64 ALU rooflines of the step: counted operations per cell-update x rate against
+    the fused multiply-add peak at the maximum SM clock seen (2 operations per FMA)."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    clk = (sm_max_mhz or 2070.0) * 1e6
+    out = {"source": "ncu SASS op counters of one step (fadd + fmul + 2 ffma; FP64 alike), peak = SMs x FMA/clk x 2 x "
+                     "max SM clock", "sms": sms, "sm_max_mhz": clk / 1e6}
+    for name, flops, value, rate in (("fp32", FLOPS_FP32_PER_CELL_UPDATE, value32, FFMA_PER_SM_CLK),
+                                     ("fp64", FLOPS_FP64_PER_CELL_UPDATE, value64, DFMA_PER_SM_CLK)):
+        if value is None:
+            continue
+        peak = sms * rate * 2 * clk / 1e12
+        got = flops * value / 1e12
+        out[name] = {"flops_per_cell_update": flops, "achieved_tflops": got, "peak_tflops": peak, "frac": got / peak}
+    return out
 
 
 def measured_peaks():
@@ -593,6 +620,7 @@ def main():
                          f"oracle (NumPy restatement of the reference, LAPACK wave speeds as in the reference), 1 core"}
 
     if rank == 0:
+        clocks = cs.summary()
         line = {
             "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -609,6 +637,7 @@ def main():
             "fp32_over_fp64": value / ws / value64,
             "l1_rho_fp32_vs_fp64": l1, "l1_after_steps": k,
             "roofline": roofline,
+            "alu_roofline": alu_roofline(value / ws, value64, (clocks or {}).get("sm_max_mhz")),
             "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1], "bookkeeping": kernel_ms[2],
                           "cell_average": kernel_ms[3]},
             "gpu_launches": sum(launches),
@@ -619,7 +648,7 @@ def main():
             "serving": serving,
             "mhd_orszag_tang": mhd,
             "sod_1d": sod,
-            "clocks": cs.summary(),
+            "clocks": clocks,
             "cpu_baseline": cpu,
             "t_simulated": clk32["t"],
         }

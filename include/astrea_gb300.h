@@ -262,14 +262,18 @@ typedef struct astrea_batch astrea_batch;
 
 /* A batch of up to max_slots grids sharing dim, model (3|8 in 1D, 4|8 in 2D),
  * precision and integrator, with stage buffers for capacity_elems elements
- * of state (the caller's arena has the same size). */
+ * of state (the caller's arena has the same size); 2D batches also hold the
+ * cell averages of their high-order grids (one arena in FP32, two in FP64). */
 int astrea_batch_create(int dim, int model, int precision, int integrator, int max_slots, long long capacity_elems,
                         astrea_batch** out);
 void astrea_batch_destroy(astrea_batch* b);
 /* Occupy ``slot`` with a grid whose nv planes start at element ``offset`` of
- * the arena; resets the slot's clock to t = 0.  ASTREA_ERR_OOM if it does not fit. */
+ * the arena; resets the slot's clock to t = 0.  ASTREA_ERR_OOM if it does not fit.
+ * Does not touch the device: the slot's descriptor and clock are written by the
+ * next astrea_batch_step / astrea_batch_graph_step / astrea_batch_clocks, on
+ * that call's stream. */
 int astrea_batch_set(astrea_batch* b, int slot, const astrea_grid* grid, long long offset);
-/* Release ``slot`` (its grid is no longer advanced). */
+/* Release ``slot`` (its grid is no longer advanced; applied like astrea_batch_set). */
 int astrea_batch_clear(astrea_batch* b, int slot);
 /* The tile in use along ``axis`` (cells along the sweep x rows across it).  A
  * batch picks it among the built candidates by timing them on its work list at

@@ -52,8 +52,10 @@ template <int MID, int DIM, int TS, int TT, typename T> constexpr size_t batch_s
   return (size_t)(m > c ? m : c);
 }
 
+// (FP64 keeps one CTA per SM here: the dispatch over six method bodies needs more registers)
 template <typename T, int MID, int DIM, int AX, int TS, int TT, int NT>
-__global__ void __launch_bounds__((NT > 256 ? NT : 256), (SweepOcc<T, MID, (NT > 256 ? NT : 256)>::value))
+__global__ void __launch_bounds__((NT > 256 ? NT : 256),
+                                  (sizeof(T) == 8 ? 1 : SweepOcc<T, MID, (NT > 256 ? NT : 256)>::value))
     batched_sweep_kernel(const BatchArgs<T> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_item;

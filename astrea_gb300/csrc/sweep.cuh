@@ -917,9 +917,11 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
 // The single-grid kernels of 2D high-order schemes stage the precomputed wS.
 template <int SCH, int DIM> constexpr bool sweep_wsin() { return DIM == 2 && SCH >= PPM; }
 
-// FP32 Euler tiles fit 1024 threads per SM (<= 64 registers); FP64 and MHD tiles are larger
+// FP32 Euler tiles fit 1024 threads per SM (<= 64 registers); FP64 Euler tiles of 256
+// threads fit two CTAs per SM (<= 128 registers); MHD tiles are larger
 template <typename T, int MID, int NT> struct SweepOcc {
-  static constexpr int value = (sizeof(T) == 4 && MID != 8) ? (1024 / NT > 0 ? 1024 / NT : 1) : 1;
+  static constexpr int value = (sizeof(T) == 4 && MID != 8) ? (1024 / NT > 0 ? 1024 / NT : 1)
+                             : ((sizeof(T) == 8 && MID != 8 && NT == 256) ? 2 : 1);
 };
 
 template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT>

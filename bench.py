@@ -58,6 +58,10 @@ SWEEP_DRAM_CELLS = 2048 * 2048
 # root are instruction sequences, which is why the FP64 step counts more operations.
 FLOPS_FP32_PER_CELL_UPDATE = 5005.1
 FLOPS_FP64_PER_CELL_UPDATE = 11979.3
+# warp instructions per cell-update of the FP32 step (smsp__inst_executed.sum, same capture):
+# against the issue rate of one warp instruction per SM sub-partition per clock
+WARP_INSTR_FP32_PER_CELL_UPDATE = 428.3
+SMSP_PER_SM = 4
 # per-SM, per-clock issue rates of the FP32 and FP64 fused multiply-add pipes on GB300
 # (ncu: sm__sass_thread_inst_executed_op_{ffma,dfma}_pred_on.sum.peak_sustained / SMs)
 FFMA_PER_SM_CLK, DFMA_PER_SM_CLK = 128, 2
@@ -158,6 +162,12 @@ def alu_roofline(value32, value64, sm_max_mhz):
         peak = sms * rate * 2 * clk / 1e12
         got = flops * value / 1e12
         out[name] = {"flops_per_cell_update": flops, "achieved_tflops": got, "peak_tflops": peak, "frac": got / peak}
+    if value32 is not None:
+        peak_issue = sms * SMSP_PER_SM * clk
+        got_issue = WARP_INSTR_FP32_PER_CELL_UPDATE * value32
+        out["issue_fp32"] = {"warp_instructions_per_cell_update": WARP_INSTR_FP32_PER_CELL_UPDATE,
+                             "achieved_per_s": got_issue, "peak_per_s": peak_issue, "frac": got_issue / peak_issue,
+                             "note": "instruction issue, the bound of this stencil"}
     return out
 
 

@@ -77,6 +77,13 @@ template <typename T> __device__ __forceinline__ T nsq3(T a, T b, T c) {
 template <typename T> __device__ __forceinline__ T norm3(T a, T b, T c) { return sqrt_((a * a + b * b) + c * c); }
 
 // ---------------------------------------------------------------- prim <-> cons (fv.py:49-53, 89-101)
+// x / (gamma - 1): FP64 divides (NumPy's rounding); FP32 multiplies by the reciprocal, which
+// the compiler forms once per kernel (gamma - 1 is a launch constant)
+template <typename T> __device__ __forceinline__ T over_gm1(T x, T gm1) {
+  if constexpr (Prec<T>::EXACT) return x / gm1;
+  else return x * (T(1) / gm1);
+}
+
 // point_convert_primitive
 template <class M, typename T> __device__ __forceinline__ void p2c(const T* w, T* q, T gm1) {
   q[0] = w[0];
@@ -84,8 +91,8 @@ template <class M, typename T> __device__ __forceinline__ void p2c(const T* w, T
   q[2] = M::VY ? w[2] * w[0] : T(0);
   q[3] = M::VZ ? w[3] * w[0] : T(0);
   T kin = w[0] * nsq_vel<M>(w);
-  if constexpr (M::MHD) q[4] = w[4] / gm1 + T(.5) * (kin + nsq_mag<M>(w));
-  else q[4] = w[4] / gm1 + T(.5) * kin;
+  if constexpr (M::MHD) q[4] = over_gm1(w[4], gm1) + T(.5) * (kin + nsq_mag<M>(w));
+  else q[4] = over_gm1(w[4], gm1) + T(.5) * kin;
   q[5] = w[5]; q[6] = w[6]; q[7] = w[7];
 }
 
@@ -141,7 +148,7 @@ template <class M, int AX, typename T> __device__ __forceinline__ void make_flux
     F[o + 1] = rv * w[1 + o] - w[5 + a] * w[5 + o];
     F[p + 1] = rv * w[1 + p] - w[5 + a] * w[5 + p];
     T vB = (w[1] * w[5] + w[2] * w[6]) + w[3] * w[7];
-    F[4] = va * ((((T(.5) * rho) * nsq_vel<M>(w)) + (gamma * P) / gm1) + nB) - w[5 + a] * vB;
+    F[4] = va * ((((T(.5) * rho) * nsq_vel<M>(w)) + over_gm1(gamma * P, gm1)) + nB) - w[5 + a] * vB;
     F[o + 5] = w[5 + o] * va - w[5 + a] * w[1 + o];
     F[p + 5] = w[5 + p] * va - w[5 + a] * w[1 + p];
     F[a + 5] = T(0);
@@ -149,7 +156,7 @@ template <class M, int AX, typename T> __device__ __forceinline__ void make_flux
     F[a + 1] = rho * (va * va) + P;
     F[o + 1] = (Has<M, 1 + o>::value) ? rv * w[1 + o] : T(0);
     F[p + 1] = (Has<M, 1 + p>::value) ? rv * w[1 + p] : T(0);
-    F[4] = va * (((T(.5) * rho) * nsq_vel<M>(w)) + (gamma * P) / gm1);
+    F[4] = va * (((T(.5) * rho) * nsq_vel<M>(w)) + over_gm1(gamma * P, gm1));
     F[5] = F[6] = F[7] = T(0);
   }
 }
@@ -222,9 +229,17 @@ __device__ __forceinline__ void hllc(int label, int physical, T gamma, const T* 
   else { uL = wm[1]; uR = wp[1]; }
   const T cL = sqrt_(gamma * dvd(pL, rL)), cR = sqrt_(gamma * dvd(pR, rR));
   const T sqL = sqrt_(rL), sqR = sqrt_(rR);
-  const T u_hat = dvd(uL * sqL + uR * sqR, sqL + sqR);
-  const T c2_hat = dvd(sqL * (cL * cL) + sqR * (cR * cR), sqL + sqR)
-                 + (T(.5) * ((uR - uL) * (uR - uL))) * dvd(sqL * sqR, (sqL + sqR) * (sqL + sqR));
+  T u_hat, c2_hat;
+  if constexpr (Prec<T>::EXACT) {
+    u_hat = dvd(uL * sqL + uR * sqR, sqL + sqR);
+    c2_hat = dvd(sqL * (cL * cL) + sqR * (cR * cR), sqL + sqR)
+           + (T(.5) * ((uR - uL) * (uR - uL))) * dvd(sqL * sqR, (sqL + sqR) * (sqL + sqR));
+  } else {
+    // FP32: one reciprocal of the weight sum for the three Roe-weighted terms
+    const T sw = sqL + sqR, inv = sw != T(0) ? T(1) / sw : T(0);
+    u_hat = (uL * sqL + uR * sqR) * inv;
+    c2_hat = (sqL * (cL * cL) + sqR * (cR * cR)) * inv + (T(.5) * ((uR - uL) * (uR - uL))) * ((sqL * sqR) * (inv * inv));
+  }
   const T ch = sqrt_(c2_hat);
   const T sL = npmin(uL - cL, u_hat - ch);
   const T sR = npmax(uR + cR, u_hat + ch);

@@ -14,7 +14,9 @@
 //
 // and then either stores the divergence (first sweep of a stage) or adds the
 // other sweep's divergence and applies the Runge-Kutta stage combine
-// (last sweep of a stage).  Every level is held at *virtual* indices; an
+// (last sweep of a stage).  2D high-order tiles of the single-grid and batched
+// engines start at wS instead: a per-stage pre-pass (cellavg.cuh) forms it once
+// for both sweeps, and the tile stages it (WSIN).  Every level is held at *virtual* indices; an
 // access at virtual v of a level is served by the value at rho(v) (clamp for
 // outflow), which is the reference's per-intermediate np.pad.
 #pragma once

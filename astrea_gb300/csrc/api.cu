@@ -887,6 +887,16 @@ int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* d
   return ASTREA_OK;
 }
 
+int astrea_clock_async(astrea_handle* h, double* t, int* steps, int* done, void* stream) {
+  if (!h || !t || !steps || !done) return fail(ASTREA_ERR_ARG, "NULL argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const Clock* c = h->eng->clk;
+  CK(cudaMemcpyAsync(t, &c->t, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(steps, &c->steps, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(done, &c->done, sizeof(int), cudaMemcpyDeviceToHost, st));
+  return ASTREA_OK;
+}
+
 int astrea_space(astrea_handle* h, const void* state, int order, void* flux_ax0, void* flux_ax1, double* eigmax,
                  void* stream) {
   if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");

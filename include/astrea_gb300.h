@@ -137,6 +137,14 @@ int astrea_step_timed(astrea_handle* h, void* state, int nsteps, double* kernel_
  * one).  No counterpart in the reference. */
 int astrea_sweep_tile(const astrea_handle* h, int axis, int* ts, int* tt);
 
+/* Enqueue on ``stream`` copies of the device clock's time, completed step
+ * count and done flag into caller memory (page-locked memory keeps them
+ * asynchronous), so that a snapshot can be labelled with its t without
+ * waiting for the stream; the values are valid once the stream has passed
+ * this point.  No counterpart in the reference (its t is a host variable,
+ * astrea.py:44-84). */
+int astrea_clock_async(astrea_handle* h, double* t, int* steps, int* done, void* stream);
+
 /* Read the device clock (synchronises ``stream``).  status bit 0: a
  * non-finite wave speed or dt was seen. */
 int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* done, int* status, void* stream);

@@ -433,6 +433,49 @@ def sod_point(n):
     return w
 
 
+def snapshot_leg(n=512, steps=240, every=20):
+    """Cost of the reference's per-step snapshots (astrea.py:47-50) when they are written while the
+    device keeps stepping: the headline method at n^2, FP32, with and without snapshots."""
+    import shutil
+    import tempfile
+    import torch
+    from astrea_gb300 import snapshots
+    from astrea_gb300.solver import Solver
+    cfg = run_config(n, 32)
+    w0 = shear_layer(n)
+
+    def fresh():
+        s = Solver(cfg)
+        s.initialise(w0)
+        s.reset_clock()
+        s.step(3, graph=True)
+        s.reset_clock()
+        torch.cuda.synchronize()
+        return s
+
+    s = fresh()
+    t0 = time.perf_counter()
+    s.step(steps, graph=True)
+    torch.cuda.synchronize()
+    plain = time.perf_counter() - t0
+    s = fresh()  # (t_end = 1 is far off: the run is bounded by max_snapshots)
+    d = tempfile.mkdtemp(prefix="astrea_snap_")
+    try:
+        store = snapshots.DirectoryStore(d, snapshots.new_file_attrs())
+        t0 = time.perf_counter()
+        written = snapshots.run_with_snapshots(s, store, "run", every=every, max_snapshots=steps // every)
+        torch.cuda.synchronize()
+        snap = time.perf_counter() - t0
+        nbytes = sum(os.path.getsize(os.path.join(d, "run", f)) for f in os.listdir(os.path.join(d, "run"))
+                     if f.endswith(".npy"))
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {"workload": f"{n}^2 headline method, FP32, {steps} steps, a primitive snapshot every {every} steps "
+                        f"(.npy store on the box's disk; the reference writes gzip HDF5 every step)",
+            "steps_per_s_plain": steps / plain, "steps_per_s_with_snapshots": len(written) * every / snap,
+            "snapshots": len(written), "snapshot_mb": nbytes / 1e6}
+
+
 def sod_leg(n=4096):
     """The plain method (FP64, reference quirks kept) on the 1D Sod problem to t = 0.2 through Solver.run."""
     import torch
@@ -627,7 +670,7 @@ def main():
     del s32
     torch.cuda.empty_cache()
 
-    batched = serving = mhd = sod = sod_state = None
+    batched = serving = mhd = sod = sod_state = snaps = None
     if not args.no_extras:
         batched = batched_leg(args.batch_steps, 2)
         torch.cuda.empty_cache()
@@ -636,6 +679,8 @@ def main():
         mhd = mhd_leg(args.mhd_n, args.mhd_steps)
         torch.cuda.empty_cache()
         sod, sod_state = sod_leg(args.sod_n)
+        torch.cuda.empty_cache()
+        snaps = snapshot_leg()
 
     cpu = None
     if rank == 0 and not args.no_cpu and sod is not None:
@@ -681,6 +726,7 @@ def main():
             "serving": serving,
             "mhd_orszag_tang": mhd,
             "sod_1d": sod,
+            "snapshots": snaps,
             "clocks": clocks,
             "cpu_baseline": cpu,
             "t_simulated": clk32["t"],

@@ -92,3 +92,31 @@ def test_arena_copies_count_the_cell_average_arenas():
     assert arena_copies(1, 32) == ARENA_COPIES and arena_copies(1, 64) == ARENA_COPIES
     assert arena_copies(2, 32) == ARENA_COPIES + 1
     assert arena_copies(2, 64) == ARENA_COPIES + 2
+
+
+def test_poll_size_follows_the_nearest_completion():
+    from astrea_gb300.serving import Request, Server
+    srv = Server.__new__(Server)  # the poll rule only, no device
+    srv.steps_per_poll, srv.max_steps_per_poll = 8, 32
+    cls = (2, 4)
+    h = 2.0 ** -10  # binary fractions keep the step counts exact
+    r1 = Request(rid=1, arrival=0, dim=2, n=64, mhd=False, scheme="ppm", solver="hllc", t_end=.5, seed=1)
+    r2 = Request(rid=2, arrival=0, dim=2, n=64, mhd=False, scheme="ppm", solver="hllc", t_end=.125, seed=2)
+    srv.active = {cls: {0: (r1, 0, 1), 1: (r2, 1, 1)}}
+    srv.last_clk = {}
+    assert srv._poll_steps(cls) == 8  # no clock reading yet
+    clk = {"t": np.array([.25, .125 - 10 * h]), "dt": np.array([16 * h, h]), "steps": np.array([10, 90]),
+           "done": np.array([0, 0])}
+    srv.last_clk = {cls: (clk, {0: 1, 1: 2})}
+    assert srv._poll_steps(cls) == 10  # r2 needs 10 more steps
+    clk["t"][1] = .125 - h / 2
+    assert srv._poll_steps(cls) == 1  # the rounded-up remainder
+    clk["dt"][1] = 0.
+    assert srv._poll_steps(cls) == 1  # a zero step: poll every step (the stall rule retires it)
+    clk["t"][1], clk["dt"][1] = 0., 2.0 ** -20
+    assert srv._poll_steps(cls) == 16  # r1's 16 steps come first
+    clk["t"][0] = 0.
+    assert srv._poll_steps(cls) == 32  # both far off: the cap
+    srv.active[cls][1] = (Request(rid=3, arrival=0, dim=2, n=64, mhd=False, scheme="plm", solver="llf",
+                                  t_end=.2, seed=3), 1, 1)
+    assert srv._poll_steps(cls) == 8  # slot 1 holds a new request without a clock reading

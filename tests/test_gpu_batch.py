@@ -112,3 +112,36 @@ def test_slots_can_be_released_and_refilled_between_steps():
         s.reset_clock()
         s.step(k)
         assert torch.equal(sb.planes(slot), s.state)
+
+
+def test_batch_non_square_periodic_and_outflow_fp64_equals_alone():
+    # non-square grids of every method class, periodic and outflow, through the batched
+    # cell-average pre-pass (one warp per strip) and the single-grid one (bulk copies where
+    # the rows are whole 16-byte units, mapped loads elsewhere): bit for bit
+    rng = np.random.default_rng(9)
+    shapes = [((40, 56), "ppm", "hllc", "wrap"), ((72, 24), "weno5", "llf", "wrap"), ((30, 50), "plm", "hllc", "edge"),
+              ((50, 34), "ppm", "llf", "edge"), ((33, 45), "weno5", "hllc", "edge")]
+    cfgs, ws = [], []
+    for (n0, n1), sch, sol, bc in shapes:
+        cfgs.append(RunConfig(dim=2, n0=n0, n1=n1, model=4, precision=64, scheme=sch, solver=sol,
+                              integrator="ssprk33", boundary=bc, gamma=1.4, dx=1.0 / n1, cfl=0.4, t_end=0.25,
+                              compat=False))
+        x, y = (np.arange(n0) + .5) / n0, (np.arange(n1) + .5) / n1
+        X, Y = np.meshgrid(x, y, indexing="ij")
+        w = np.zeros((n0, n1, 8))
+        w[..., 0] = 1 + .3 * np.sin(2 * np.pi * X) * np.cos(2 * np.pi * Y) + rng.uniform(0, .05)
+        w[..., 1] = .4 * np.sin(2 * np.pi * Y)
+        w[..., 2] = -.3 * np.cos(2 * np.pi * X)
+        w[..., 4] = 1 + .2 * np.cos(2 * np.pi * (X + Y))
+        ws.append(w)
+    b = Batch(cfgs)
+    b.initialise(ws)
+    b.step(5)
+    clk = b.clocks()
+    for g, (c, w) in enumerate(zip(cfgs, ws)):
+        s = Solver(c)
+        s.initialise(w)
+        s.reset_clock()
+        s.step(5)
+        assert torch.equal(b.planes(g), s.state), g
+        assert s.clock()["t"] == clk["t"][g]

@@ -35,10 +35,20 @@ def test_fp64_update_keeps_mirror_symmetry_at_full_size(scheme, solver, dissipat
                     boundary="wrap", gamma=1.4, dx=1.0 / N, cfl=0.8, t_end=1.0, compat=False, flatten=dissipation,
                     viscosity=dissipation)
     w = blast(N)
-    assert np.array_equal(w[..., 0], w[..., 0].T) and np.array_equal(w[..., 1], w[..., 2].T)
+    # conservative state loaded as is (the centre -> average conversion of ``initialise`` adds
+    # the two axes' corrections in a fixed order, which is not mirror-symmetric in the last bit)
+    q0 = np.zeros_like(w)
+    q0[..., 0] = w[..., 0]
+    q0[..., 1] = w[..., 0] * w[..., 1]
+    q0[..., 2] = w[..., 0] * w[..., 2]
+    q0[..., 4] = w[..., 4] / .4 + .5 * w[..., 0] * (w[..., 1] ** 2 + w[..., 2] ** 2)
+    assert np.array_equal(q0[..., 0], q0[..., 0].T) and np.array_equal(q0[..., 1], q0[..., 2].T)
+    assert np.array_equal(q0[..., 4], q0[..., 4].T)
     s = Solver(cfg)
-    s.initialise(w)
+    s.load_conservative(q0)
     s.reset_clock()
+    q = s.state
+    assert torch.equal(q[0], q[0].T) and torch.equal(q[1], q[2].T)
     s.step(3)
     assert s.clock()["status"] == 0
     q = s.state  # planes rho, m_x, m_y, E

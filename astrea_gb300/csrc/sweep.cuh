@@ -118,6 +118,11 @@ template <typename T, int SCH, int DIM, int AX, int TS, int TT, int NV> struct T
     return DYN ? ((t0 - G::WT) / A) * A : t0 + XB;  // t0 - WT >= 0 whenever the box is used
   }
   __host__ __device__ static int xoff(int t0) { return DYN ? (t0 - G::WT) - x0(0, t0) : XOFF; }
+  // the box of the tile at (s0, t0) lies inside an n0 x n1 grid
+  __host__ __device__ static bool inside(int s0, int t0, int n0, int n1) {
+    return AX == 1 ? (s0 + XB >= 0 && s0 + XB + BW <= n1 && t0 - G::WT >= 0 && t0 - G::WT + BH <= n0)
+                   : (t0 - G::WT >= 0 && x0(s0, t0) + BW <= n1 && s0 + G::W_BEG >= 0 && s0 + G::W_BEG + BH <= n0);
+  }
 };
 
 // The TMA box of the viscous strip of a WSIN PPM tile: the state on cells
@@ -898,11 +903,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
   if constexpr (TMA_OK && DIM == 2 && (WSIN || !G::HO)) {
     using B = TmaBox<T, SCH, DIM, AX, TS, TT, Model<MID>::NV>;
     if constexpr ((size_t)S::n_R * sizeof(T) >= (size_t)B::BYTES + 128) {
-      const bool box_in = a.tmaps != nullptr &&
-                          (AX == 1 ? (s0 + B::XB >= 0 && s0 + B::XB + B::BW <= a.n1 && t0 - G::WT >= 0 &&
-                                      t0 - G::WT + B::BH <= a.n0)
-                                   : (t0 - G::WT >= 0 && B::x0(s0, t0) + B::BW <= a.n1 && s0 + G::W_BEG >= 0 &&
-                                      s0 + G::W_BEG + B::BH <= a.n0));
+      const bool box_in = a.tmaps != nullptr && B::inside(s0, t0, a.n0, a.n1);
       if (box_in) {
         sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, true, WSIN>(a, s0, t0, smem_raw);
         return;

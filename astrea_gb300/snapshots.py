@@ -16,8 +16,9 @@ same sequence of snapshots without stopping the device:
 
 Stores: ``HDF5Store`` writes the reference's layout with h5py where it is
 installed; ``DirectoryStore`` writes the same groups, names and attributes as
-a directory tree (``attrs.json``, ``<group>/attrs.json``, ``<group>/index.json``
-and one ``.npy`` per dataset) where it is not.
+a directory tree (``attrs.json``, ``<group>/attrs.json``, ``<group>/index.jsonl``
+with one line per dataset in write order, and one ``.npy`` per dataset) where
+it is not.
 """
 
 import ctypes
@@ -40,7 +41,6 @@ class DirectoryStore:
     def __init__(self, path, file_attrs=None):
         self.path = path
         os.makedirs(path, exist_ok=True)
-        self._index = {}
         self._write_json(os.path.join(path, "attrs.json"), file_attrs or {})
 
     @staticmethod
@@ -53,13 +53,13 @@ class DirectoryStore:
     def create_group(self, key, attrs):
         os.makedirs(os.path.join(self.path, key), exist_ok=True)
         self._write_json(os.path.join(self.path, key, "attrs.json"), attrs)
-        self._index[key] = []
-        self._write_json(os.path.join(self.path, key, "index.json"), [])
+        open(os.path.join(self.path, key, "index.jsonl"), "w").close()
 
     def write(self, key, name, array, attrs):
+        # the array first, then its index line: a reader never sees a line without its data
         np.save(os.path.join(self.path, key, name + ".npy"), array)
-        self._index[key].append({"name": name, "attrs": attrs})
-        self._write_json(os.path.join(self.path, key, "index.json"), self._index[key])
+        with open(os.path.join(self.path, key, "index.jsonl"), "a") as f:
+            f.write(json.dumps({"name": name, "attrs": attrs}) + "\n")
 
     def close(self):
         pass
@@ -103,8 +103,8 @@ def open_store(path, file_attrs=None):
 
 def read_directory_run(path, key):
     """[(name, attrs, array)] of one run of a ``DirectoryStore``, in write order."""
-    with open(os.path.join(path, key, "index.json")) as f:
-        index = json.load(f)
+    with open(os.path.join(path, key, "index.jsonl")) as f:
+        index = [json.loads(line) for line in f if line.strip()]
     return [(e["name"], e["attrs"], np.load(os.path.join(path, key, e["name"] + ".npy"))) for e in index]
 
 

@@ -12,7 +12,9 @@ template <typename T> using SweepFn = cudaError_t (*)(const SweepArgs<T>&, cudaS
 // engine's autotuner: 32 (sweep) x 8 (rows) x 256 threads, and 32 x 15 x 512
 // threads (fewer transverse halo rows per cell, same threads per SM, and the
 // 15 x 33 interfaces of the second face level fit one pass of 512 threads;
-// FP32 Euler tiles only, whose shared memory and 64 registers allow it).
+// Euler tiles only: two CTAs per SM in FP32 at 64 registers, one in FP64 at
+// 122 registers and 182 KB of shared memory, where fewer halo cells per cell
+// matter because the FP64 pipe bounds the kernel).
 constexpr int TS1 = 32, NT1 = 64;
 constexpr int NTILES2 = 2;
 template <int I> struct Tile2;
@@ -52,7 +54,7 @@ template <typename T, int MID, int SCH, int SOL, int DIM, int AX> SweepFn<T> swe
     return tile == 0 ? &launch_sweep<T, MID, SCH, SOL, 1, 0, TS1, 1, NT1> : nullptr;
   } else {
     if (tile == 0) return &launch_sweep<T, MID, SCH, SOL, 2, AX, Tile2<0>::TS, Tile2<0>::TT, Tile2<0>::NT>;
-    if constexpr (sizeof(T) == 4 && MID != 8) {
+    if constexpr (MID != 8) {
       if (tile == 1) return &launch_sweep<T, MID, SCH, SOL, 2, AX, Tile2<1>::TS, Tile2<1>::TT, Tile2<1>::NT>;
     }
     return nullptr;

@@ -55,7 +55,9 @@ SWEEP_DRAM_CELLS = 2048 * 2048
 # Floating-point operations per cell-update of one SSPRK3 step (every kernel of the step),
 # from ncu's SASS op counters (fadd + fmul + 2 x ffma, and the FP64 counterparts) over one
 # step of the workload at 512^2 (profiles/flops_step_2d_shear.md).  FP64 division and square
-# root are instruction sequences, which is why the FP64 step counts more operations.
+# root are instruction sequences, which is why the FP64 step counts more operations.  The FP64
+# count was taken with the 32 x 8 FP64 tile; where the autotuner picks the 32 x 15 tile the step
+# recomputes fewer halo cells, so the reported FP64 fraction is an upper estimate.
 FLOPS_FP32_PER_CELL_UPDATE = 5005.1
 FLOPS_FP64_PER_CELL_UPDATE = 11979.3
 # warp instructions per cell-update of the FP32 step (smsp__inst_executed.sum, same capture):

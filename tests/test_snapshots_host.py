@@ -4,6 +4,7 @@ import json
 import os
 
 import numpy as np
+import pytest
 
 from astrea_gb300 import snapshots
 from astrea_gb300.solver import RunConfig
@@ -50,3 +51,73 @@ def test_open_store_falls_back_to_a_directory(tmp_path):
         assert isinstance(st, snapshots.HDF5Store)
     except ImportError:
         assert isinstance(st, snapshots.DirectoryStore) and os.path.isdir(tmp_path / "out.h5.d")
+
+
+class _FakeEvent:
+    def record(self, stream=None):
+        pass
+
+    def synchronize(self):
+        pass
+
+
+class _FakeStream:
+    def wait_event(self, ev):
+        pass
+
+
+class _FakeSolver:
+    """A 'grid' on the host whose clock advances by a fixed dt per step (clipped onto t_end); the
+    stand-in library writes its primitives and clock through the same pointers the device path uses."""
+
+    def __init__(self, cfg, dt):
+        import ctypes
+        import torch
+        self.cfg, self.dt = cfg, dt
+        self.state = torch.arange(cfg.model * cfg.n0 * cfg.n1, dtype=torch.float64).reshape(cfg.model, cfg.n0, cfg.n1)
+        self.t, self.steps, self.handle = 0.0, 0, None
+        solver = self
+
+        class Lib:
+            def astrea_to_primitive(self, h, state, out, stream):
+                src = (solver.state + solver.t).contiguous()  # held until the copy is done
+                ctypes.memmove(out.value, src.data_ptr(), src.numel() * 8)
+                return 0
+
+            def astrea_clock_async(self, h, t, steps, done, stream):
+                ctypes.memmove(t.value, ctypes.byref(ctypes.c_double(solver.t)), 8)
+                ctypes.memmove(steps.value, ctypes.byref(ctypes.c_int(solver.steps)), 4)
+                ctypes.memmove(done.value, ctypes.byref(ctypes.c_int(int(solver.t >= solver.cfg.t_end))), 4)
+                return 0
+
+        self.lib = Lib()
+
+    def step(self, n=1, graph=True):
+        for _ in range(n):
+            if self.t >= self.cfg.t_end:
+                return
+            self.t = self.cfg.t_end if self.t + self.dt >= self.cfg.t_end * (1 - 1e-12) else self.t + self.dt
+            self.steps += 1
+
+
+def test_snapshot_loop_sequence_on_the_host(tmp_path, monkeypatch):
+    import torch
+    monkeypatch.setattr(torch.Tensor, "pin_memory", lambda self: self)
+    monkeypatch.setattr(torch.cuda, "Stream", lambda *a, **k: _FakeStream())
+    monkeypatch.setattr(torch.cuda, "Event", lambda *a, **k: _FakeEvent())
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda *a, **k: None)
+    monkeypatch.setattr(torch.cuda, "stream", lambda s: __import__("contextlib").nullcontext())
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda *a, **k: None)
+    monkeypatch.setattr(snapshots, "_stream", lambda: None)
+    cfg = RunConfig(dim=2, n0=6, n1=5, model=4, precision=64, scheme="ppm", solver="hllc", integrator="ssprk33",
+                    boundary="wrap", gamma=1.4, dx=.2, cfl=.8, t_end=.25)
+    for every, expect_t in ((1, [0, .1, .2, .25]), (2, [0, .2, .25])):
+        s = _FakeSolver(cfg, dt=.1)
+        st = snapshots.DirectoryStore(str(tmp_path / f"e{every}"))
+        written = snapshots.run_with_snapshots(s, st, "run", every=every)
+        run = snapshots.read_directory_run(str(tmp_path / f"e{every}"), "run")
+        assert [w[0] for w in written] == pytest.approx(expect_t)
+        assert [r[0] for r in run] == [str(float(t)) for t, _ in written]
+        for (name, attrs, arr), (t, _) in zip(run, written):
+            # the snapshot of time t is the state at t, in the reference layout
+            assert arr.shape == (6, 5, 8) and arr[0, 0, 0] == pytest.approx(t)

@@ -7,10 +7,11 @@
 //
 // The two sweeps add the two axes' corrections in opposite orders, which round
 // differently, so the kernel writes one copy per sweep: w_ax0 for the axis-0
-// sweep (axis 0 first), w_ax1 for the axis-1 sweep (FP64; see below for FP32).  Edge cells take their
-// neighbours through the input boundary map (clamp for outflow, wrap for
-// periodic), the values the sweep tiles' own q level holds there.  The
-// arithmetic is the sweep's, operation for operation.
+// sweep (axis 0 first), w_ax1 for the axis-1 sweep (FP64; see below for
+// FP32).  Edge cells take their neighbours through the input boundary map
+// (clamp for outflow, wrap for periodic): the values a sweep tile's own q
+// level holds there where it forms wS itself (1D and low-order tiles).  The
+// arithmetic is that per-tile formation's, operation for operation.
 #pragma once
 #include "batch.cuh"
 

@@ -9,9 +9,10 @@
 // differently, so the kernel writes one copy per sweep: w_ax0 for the axis-0
 // sweep (axis 0 first), w_ax1 for the axis-1 sweep (FP64; see below for
 // FP32).  Edge cells take their neighbours through the input boundary map
-// (clamp for outflow, wrap for periodic): the values a sweep tile's own q
-// level holds there where it forms wS itself (1D and low-order tiles).  The
-// arithmetic is that per-tile formation's, operation for operation.
+// (clamp for outflow, wrap for periodic), the values a sweep tile's q level
+// holds there when the tile forms wS itself (the per-tile path of sweep.cuh,
+// which 1D tiles still take).  The arithmetic is that path's, operation for
+// operation.
 #pragma once
 #include "batch.cuh"
 

@@ -331,6 +331,42 @@ def batched_leg(steps, warmup, ngrids=512, seed=SEED):
     return out
 
 
+def batched_cpu_worker(args):
+    """One SSPRK3 step of one four-quadrant grid of the batched workload with the oracle (LAPACK
+    wave speeds as the reference); returns the seconds it took."""
+    n, ppm, seed = args
+    import numpy as np_
+    sys.path.insert(0, ROOT)
+    from oracle import stepper
+    from astrea_gb300.serving import Request
+    r = Request(rid=0, arrival=0.0, dim=2, n=n, mhd=False, scheme="plm", solver="llf", t_end=.25, seed=seed)
+    cfg = stepper.OracleConfig(dim=2, scheme="ppm" if ppm else "plm", solver="hllc" if ppm else "llf",
+                               integrator="ssprk33", gamma=1.4, bc="edge", dx=1.0 / n, cfl=0.8, eig="lapack",
+                               t_end=0.25, compat=False)
+    q = stepper.initialise(r.initial_state(), cfg)
+    t0 = time.perf_counter()
+    with np_.errstate(all="ignore"):
+        stepper.step(q, cfg, 0.0, 1, [0, 1])
+    return time.perf_counter() - t0
+
+
+def batched_cpu_baseline(n=128, seed=SEED):
+    """The batched workload's methods on the host cores: one process per core, each one SSPRK3 step
+    of an independent 128^2 four-quadrant grid (half PLM+LLF, half PPM+HLLC), oracle."""
+    import multiprocessing as mp
+    procs = max(1, len(os.sched_getaffinity(0)))
+    rng = np.random.default_rng(seed)
+    jobs = [(n, k % 2 == 1, int(rng.integers(1 << 31))) for k in range(procs)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        pool.map(batched_cpu_worker, [(16, False, 1)] * procs)  # start the workers and their imports
+        t0 = time.perf_counter()
+        pool.map(batched_cpu_worker, jobs)
+        wall = time.perf_counter() - t0
+    return {"value": procs * n * n / wall, "unit": "cell-updates/s", "cores": procs, "kind": "port",
+            "sample": f"{procs} processes, each one SSPRK3 step of an independent {n}^2 four-quadrant grid of the "
+                      f"workload (PLM+LLF or PPM+HLLC), oracle with LAPACK wave speeds as in the reference"}
+
+
 def batched_fp64_check(cfgs, seeds, steps, count=32):
     """Per-instance FP32-vs-FP64 L1(rho) of the first ``count`` batched grids after ``steps`` steps."""
     import torch
@@ -693,6 +729,8 @@ def main():
         else:
             sod = sod_out
         snaps = leg(snapshot_leg)
+        if rank == 0 and not args.no_cpu and isinstance(batched, dict) and "value" in batched:
+            batched["cpu_baseline"] = leg(batched_cpu_baseline)
 
     cpu = None
     if rank == 0 and not args.no_cpu and sod_state is not None:

@@ -29,3 +29,9 @@ def test_minimum_traffic_and_constants_are_consistent():
     alg = 2048 * 2048 * 4 * 4 * (2 + 2 + (2 + 5) + (2 + 5)) / 6
     assert 0.9 * alg < bench.SWEEP_DRAM_BYTES < 1.2 * alg
     assert bench.FLOPS_FP64_PER_CELL_UPDATE > bench.FLOPS_FP32_PER_CELL_UPDATE > 0
+
+
+def test_batched_cpu_worker_runs_the_workload_methods():
+    # one oracle step of a small four-quadrant grid with each of the batched workload's methods
+    for ppm in (False, True):
+        assert bench.batched_cpu_worker((16, ppm, 7)) > 0

@@ -17,7 +17,7 @@ EXPORTS = [
     "astrea_reset_clock", "astrea_step", "astrea_graph_step", "astrea_get_clock", "astrea_space", "astrea_time",
     "astrea_to_primitive", "astrea_reduce_conserved", "astrea_step_timed", "astrea_reduce_conserved_static",
     "astrea_sweep_tile", "astrea_point_state", "astrea_total_variation", "astrea_solution_error",
-    "astrea_clock_async",
+    "astrea_clock_async", "astrea_space_ct",
 ]
 
 
@@ -65,6 +65,7 @@ def load(path=LIB_PATH):
             "astrea_get_clock": ([vp, dp, dp, ip, ip, ip, vp], i),
             "astrea_clock_async": ([vp, vp, vp, vp, vp], i),
             "astrea_space": ([vp, vp, i, vp, vp, dp, vp], i),
+            "astrea_space_ct": ([vp, vp, i, vp, vp, dp, vp, vp, vp, vp], i),
             "astrea_time": ([vp, vp, d, i, vp], i),
             "astrea_to_primitive": ([vp, vp, vp, vp], i),
             "astrea_reduce_conserved": ([vp, vp, dp, vp], i),

@@ -99,7 +99,8 @@ struct IEngine {
   }
   virtual int alloc() = 0;
   virtual int enqueue_step(void* state, Clock* c, bool device_dt, cudaStream_t st, KTimer* tm = nullptr) = 0;
-  virtual int space(const void* state, int order, void* f0, void* f1, double* eigmax, cudaStream_t st) = 0;
+  virtual int space(const void* state, int order, void* f0, void* f1, double* eigmax, cudaStream_t st,
+                    void* face0 = nullptr, void* face1 = nullptr, void* corner = nullptr) = 0;
   virtual int initialise(const void* prim, void* out, cudaStream_t st) = 0;
   virtual int to_primitive(const void* state, void* out, cudaStream_t st) = 0;
   virtual int reduce(const void* state, double* host, cudaStream_t st) = 0;
@@ -250,7 +251,7 @@ template <typename T> struct Engine final : IEngine {
       default: return fail(ASTREA_ERR_CONFIG, "unknown scheme");
     }
     for (int ax = 0; ax < cfg.dim; ++ax)
-      for (int t = 0; t < NTILES2; ++t) cand[ax][t] = getter(cfg.model, cfg.solver, cfg.dim, ax, t);
+      for (int t = 0; t < NTILES2; ++t) cand[ax][t] = getter(cfg.model, cfg.solver == LW ? LLF : cfg.solver, cfg.dim, ax, t);
     sweep[0] = cand[0][0];
     sweep[1] = cfg.dim == 2 ? cand[1][0] : nullptr;
     if (!sweep[0] || (cfg.dim == 2 && !sweep[1]))
@@ -404,6 +405,7 @@ template <typename T> struct Engine final : IEngine {
     a.dx = cfg.dx;
     a.clock = c;
     a.physical = (cfg.flags & ASTREA_FLAG_PHYSICAL) ? 1 : 0;
+    a.lw = cfg.solver == LW ? 1 : 0;
     a.flatten = (cfg.flags & ASTREA_FLAG_FLATTEN) ? 1 : 0;
     a.viscosity = (cfg.flags & ASTREA_FLAG_VISCOSITY) ? 1 : 0;
     a.av_alpha = T(0.3);
@@ -438,7 +440,7 @@ template <typename T> struct Engine final : IEngine {
     const int blocks = (int)std::min<long long>((cells + threads - 1) / threads, 152LL * 16);
     const dim3 cgrid((cfg.n0 + CTX - 1) / CTX, (cfg.n1 + CTY - 1) / CTY);
     const dim3 rgrid((cfg.n0 + RTX - 1) / RTX, (cfg.n1 + RTY - 1) / RTY);
-    const int hll = cfg.solver != LLF;
+    const int hll = cfg.solver == HLLC || cfg.solver == HLLD;
     for (int s = 0; s < ns; ++s) {
       T* cur = s == 0 ? u : k[(s - 1) % 2];
       T* out = s == ns - 1 ? u : k[s % 2];
@@ -629,7 +631,9 @@ template <typename T> struct Engine final : IEngine {
     return ASTREA_OK;
   }
 
-  int space(const void* state, int order, void* f0, void* f1, double* eigmax, cudaStream_t st) override {
+  // face0/face1/corner (constrained transport only): each sweep's face values and the corner field
+  int space(const void* state, int order, void* f0, void* f1, double* eigmax, cudaStream_t st, void* face0,
+            void* face1, void* corner) override {
     Clock* c = clk + 1;
     CK(cudaMemsetAsync(&c->emax[0], 0, 2 * sizeof(unsigned long long), st));
     CK(cudaMemcpyAsync(&c->order, &order, sizeof(int), cudaMemcpyHostToDevice, st));
@@ -638,13 +642,24 @@ template <typename T> struct Engine final : IEngine {
     a.want_emax = 1;
     a.dout = d[0];
     a.flux_out = static_cast<T*>(f0);
+    T* faces[2] = {ct() ? (face0 ? static_cast<T*>(face0) : wf[0]) : nullptr,
+                   ct() ? (face1 ? static_cast<T*>(face1) : wf[1]) : nullptr};
+    a.wface_out = faces[0];
     int prc = prep(static_cast<const T*>(state), c, st, nullptr);
     if (prc) return prc;
     CK(run_sweep(sweep[0], 0, a, st));
     if (cfg.dim == 2) {
       a.dout = d[1];
       a.flux_out = static_cast<T*>(f1);
+      a.wface_out = faces[1];
       CK(run_sweep(sweep[1], 1, a, st));
+    }
+    if (ct() && corner) {
+      const dim3 cgrid((cfg.n0 + CTX - 1) / CTX, (cfg.n1 + CTY - 1) / CTY);
+      corner_kernel<T><<<cgrid, 256, corner_smem_bytes<T>(), st>>>(faces[0], faces[1], static_cast<T*>(corner),
+                                                                   cfg.n0, cfg.n1, plane(), cfg.boundary,
+                                                                   T(cfg.gamma), cfg.solver == HLLC || cfg.solver == HLLD, c);
+      CK(cudaGetLastError());
     }
     unsigned long long e[2];
     CK(cudaMemcpyAsync(e, &c->emax[0], sizeof(e), cudaMemcpyDeviceToHost, st));
@@ -712,7 +727,7 @@ static int validate(const astrea_cfg* c) {
   if (c->model == 4 && c->dim != 2) return fail(ASTREA_ERR_CONFIG, "model 4 is 2D only");
   if (c->precision != 32 && c->precision != 64) return fail(ASTREA_ERR_CONFIG, "precision must be 32 or 64");
   if (c->scheme < 0 || c->scheme > WENO7) return fail(ASTREA_ERR_CONFIG, "unknown scheme");
-  if (c->solver < 0 || c->solver > HLLD) return fail(ASTREA_ERR_CONFIG, "unknown solver");
+  if (c->solver < 0 || c->solver > LW) return fail(ASTREA_ERR_CONFIG, "unknown solver");
   if (stages_of(c->integrator) < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this build");
   if (c->boundary != EDGE && c->boundary != WRAP) return fail(ASTREA_ERR_CONFIG, "boundary must be edge(0) or wrap(1)");
   if ((c->flags & ASTREA_FLAG_CT) && (c->dim != 2 || c->model != 8))
@@ -903,6 +918,16 @@ int astrea_space(astrea_handle* h, const void* state, int order, void* flux_ax0,
   int trc = h->eng->prepare(state, static_cast<cudaStream_t>(stream));
   if (trc) return trc;
   return h->eng->space(state, order & 1, flux_ax0, flux_ax1, eigmax, static_cast<cudaStream_t>(stream));
+}
+
+int astrea_space_ct(astrea_handle* h, const void* state, int order, void* flux_ax0, void* flux_ax1, double* eigmax,
+                    void* face_ax0, void* face_ax1, void* corner, void* stream) {
+  if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
+  if (!(h->eng->cfg.flags & ASTREA_FLAG_CT)) return fail(ASTREA_ERR_CONFIG, "astrea_space_ct needs ASTREA_FLAG_CT");
+  int trc = h->eng->prepare(state, static_cast<cudaStream_t>(stream));
+  if (trc) return trc;
+  return h->eng->space(state, order & 1, flux_ax0, flux_ax1, eigmax, static_cast<cudaStream_t>(stream), face_ax0,
+                       face_ax1, corner);
 }
 
 int astrea_time(astrea_handle* h, void* state, double dt, int order, void* stream) {

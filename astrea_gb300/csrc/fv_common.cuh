@@ -12,7 +12,8 @@ namespace astrea {
 
 // ---------------------------------------------------------------- enums (match include/astrea_gb300.h)
 enum Scheme { PCM = 0, PLM = 1, PPM = 2, WENO3 = 3, WENO5 = 4, WENO7 = 5 };
-enum Solver { LLF = 0, HLLC = 1, HLLD = 2 };
+// LW runs the LLF kernels with the Lax-Wendroff interface coefficient (SweepArgs::lw)
+enum Solver { LLF = 0, HLLC = 1, HLLD = 2, LW = 3 };
 enum Boundary { EDGE = 0, WRAP = 1 };
 enum Integrator { EULER = 0, SSPRK22 = 1, SSPRK33 = 2, SSPRK43 = 3, SSPRK53 = 4, SSPRK54 = 5, SSPRK104 = 6, RK4 = 7 };
 

@@ -143,7 +143,9 @@ static __global__ void end_step_kernel(Clock* clocks, int ngrids) {
   if (c.naxes == 2) c.order ^= 1;
   c.emax[0] = 0ull;
   c.emax[1] = 0ull;
-  if (!(c.t < c.t_end) || (c.status & 1)) c.done = 1;
+  // status bit 0: non-finite or zero dt; bit 1: a tile's bulk copy timed out (its copy may still
+  // be in flight), fatal for the grid as well
+  if (!(c.t < c.t_end) || (c.status & 3)) c.done = 1;
 }
 
 // index helpers in the physical frame: axis 0 (x, stride n1), axis 1 (y, contiguous)

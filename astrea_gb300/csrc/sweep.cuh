@@ -41,6 +41,7 @@ template <typename T> struct SweepArgs {
   int integ, stage;   // Runge-Kutta scheme and stage for the combine
   int want_emax;      // accumulate the max wave speed of this axis into the clock
   int physical;       // textbook HLLC/HLLD (label = physical axis) instead of the reference's
+  int lw;             // LLF kernels: the Lax-Wendroff coefficient v_n^2 / max|lambda| instead of max|lambda|
   T gamma, gm1;
   double dx;
   T* dout;            // mode 0: divergence output (NV planes)
@@ -352,13 +353,12 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       }
       __syncthreads();  // the barrier is initialised before anyone waits on it
       if (!strip_tma) stage_strip();
-      constexpr int kWaitLimit = 1 << 16;
-      const bool landed = mbar_wait_bounded(&s_bar, 0, kWaitLimit);
+      const bool landed = mbar_wait_timed(&s_bar, 0, kCopyWaitNs);
       if (!__syncthreads_and(landed)) {
         // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
         if (tid == 0) {
           atomicOr(&a.clock->status, 2);
-          mbar_wait_bounded(&s_bar, 0, kWaitLimit);
+          mbar_wait_timed(&s_bar, 0, kDrainWaitNs);
         }
         return;
       }
@@ -396,13 +396,12 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       else tma_load_3d(stage, map, B::x0(s0, t0), s0 + G::Q_BEG, 0, &s_bar);
     }
     __syncthreads();  // the barrier is initialised before anyone waits on it
-    constexpr int kWaitLimit = 1 << 16;
-    const bool landed = mbar_wait_bounded(&s_bar, 0, kWaitLimit);
+    const bool landed = mbar_wait_timed(&s_bar, 0, kCopyWaitNs);
     if (!__syncthreads_and(landed)) {
       // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
       if (tid == 0) {
         atomicOr(&a.clock->status, 2);
-        mbar_wait_bounded(&s_bar, 0, kWaitLimit);
+        mbar_wait_timed(&s_bar, 0, kDrainWaitNs);
       }
       return;
     }
@@ -693,7 +692,12 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         else arith_avg<M>(wp, wm, y);
       }
       const T lam = max_speed<M, DIM == 1 ? 0 : AX>(y, gamma);
-      if constexpr (LAM_ALL) s_lam[row * G::YW + col] = lam;
+      if constexpr (LAM_ALL) {
+        // Lax-Wendroff (solvers.py:79-88): the squared 'sound speed' over the largest |eigenvalue|,
+        // where the sound speed is the entropy-wave eigenvalue v_n of the interface average
+        const T vn = y[1 + (DIM == 1 ? 0 : AX)];
+        s_lam[row * G::YW + col] = a.lw ? dvd(vn * vn, lam) : lam;
+      }
       if (a.want_emax && vj >= s0 && vj < s0 + TS && vj < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) lmax = npmax(lmax, lam);
     }
     if (a.want_emax) block_max_to_clock(lmax, &a.clock->emax[DIM == 1 ? 0 : AX]);

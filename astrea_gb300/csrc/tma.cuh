@@ -2,9 +2,12 @@
 // issues a 3D bulk tensor copy of the tile's conservative state (all variable
 // planes, halos included) into shared memory, completing on an mbarrier.
 //
-// Every wait is bounded: a copy that does not land within the limit sets bit 1
-// of the grid clock's status, and the CTA stops after waiting (bounded again)
-// for the copy it issued.
+// Every wait is bounded in wall time (the %globaltimer nanosecond clock, with
+// an iteration cap besides): a copy that does not land within 2 ms sets bit 1
+// of the grid clock's status, and the CTA stops after waiting up to 50 ms more
+// for the copy it issued.  A copy that has still not landed then may write into
+// shared memory that a later CTA is given, so a status with bit 1 set is fatal
+// for the grid: the host stops stepping it.
 #pragma once
 #include <cuda.h>
 
@@ -43,10 +46,24 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
   return done != 0;
 }
 
-// bounded wait for phase ``parity`` of the barrier; false if the limit ran out
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity, int limit) {
-  for (int i = 0; i < limit; ++i)
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// wait for phase ``parity`` of the barrier for at most ``limit_ns`` nanoseconds of wall
+// time (and at most 2^24 polls); false if the limit ran out
+constexpr unsigned long long kCopyWaitNs = 2000000ull;      // a tile's bulk copy: 2 ms (it takes microseconds)
+constexpr unsigned long long kDrainWaitNs = 50000000ull;    // after a timeout, for the copy in flight: 50 ms
+__device__ __forceinline__ bool mbar_wait_timed(unsigned long long* bar, unsigned parity,
+                                                unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer_ns();
+  for (int i = 0; i < (1 << 24); ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 15) == 15 && globaltimer_ns() - t0 > limit_ns) return false;
+  }
   return false;
 }
 

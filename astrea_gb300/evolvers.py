@@ -8,11 +8,17 @@ and the result has the reference's shapes:
 
 * evolve_space -> ``{axes: {'flux': interface fluxes in the sweep frame,
   'eigmax': float}}`` keyed and ordered like ``sim_variables.permutations``;
+  with ``sim_variables.magnetic_2d`` each entry also carries ``'face_avg'``
+  (the sweep's face values in the sweep frame) and ``'mag_corner'`` (the
+  corner electric field, transposed per axis as evolvers.py:28-32 stores it);
 * evolve_time  -> the updated grid.
 
 ``core_run``'s use of ``fluxes`` is only ``eigmax`` (astrea.py:70); the fluxes
 of the initial state are recomputed on the device inside evolve_time (they are
 a pure function of ``grid``), so ``fluxes`` may come from either evolver.
+With ``magnetic_2d``, evolve_time also does what the reference does to its
+input (evolvers.py:73-76): the caller's ``grid`` has its B_x / B_y components
+overwritten by the face-averaged values of ``fluxes[axes]['face_avg']``.
 
 ``simulate`` is the core_run loop (astrea.py:44-85) on the device without the
 per-step HDF5 snapshot.
@@ -58,11 +64,21 @@ def evolve_space(grid, sim_variables, precision=64):
     """Interface fluxes and max wave speeds of every axis (evolvers.py:12-34)."""
     s = _solver_for(grid, sim_variables, precision)
     s.load_conservative(grid)
-    (f0, f1), eig = s.space(_order(sim_variables))
+    magnetic = s.cfg.magnetic_2d
+    if magnetic:
+        (f0, f1), eig, faces, corner = s.space_ct(_order(sim_variables))
+    else:
+        (f0, f1), eig = s.space(_order(sim_variables))
     out = {}
     for axis, axes in sim_variables.permutations.items():
         F = f0 if axis == 0 else f1
         out[axes] = {"flux": _like(_flux_aos(F, s.cfg.model, s.cfg.dim), grid), "eigmax": float(eig[axis])}
+        if magnetic:
+            # face values in the sweep frame (data[axes]['wF']); the corner field as evolvers.py:28-32
+            # stores it: its transpose for the axis-0 sweep, itself for the axis-1 sweep
+            face = faces[axis].permute(1, 2, 0)
+            out[axes]["face_avg"] = _like(face if axis == 0 else face.transpose(0, 1), grid)
+            out[axes]["mag_corner"] = _like(corner.t() if axis == 0 else corner, grid)
     return out
 
 
@@ -71,7 +87,16 @@ def evolve_time(grid, fluxes, dt, sim_variables, precision=64):
     s = _solver_for(grid, sim_variables, precision)
     s.load_conservative(grid)
     s.time(float(dt), _order(sim_variables))
-    return _like(s.conservative(), grid)
+    new = _like(s.conservative(), grid)
+    if s.cfg.magnetic_2d:
+        # the reference re-assigns the B components of its input grid to the face averages
+        # (evolvers.py:73-76) before stepping; its caller sees that change
+        for axis, axes in sim_variables.permutations.items():
+            face = fluxes.get(axes, {}).get("face_avg")
+            if face is not None:
+                back = face.transpose(1, 0, 2) if isinstance(face, np.ndarray) else face.transpose(0, 1)
+                grid[..., 5 + axis] = (face if axis == 0 else back)[..., 5 + axis]
+    return new
 
 
 def simulate(sim_variables, grid0, precision=64, max_steps=None, graph=True):

@@ -180,7 +180,8 @@ def stalled(steps, t, dt, t_end, max_steps, check_after=1000):
 @dataclass
 class ServeStats:
     latencies_ms: list = field(default_factory=list)
-    cell_updates: float = 0.0
+    cell_updates: float = 0.0         # of requests that finished with status 0
+    failed_cell_updates: float = 0.0  # spent on requests retired with a non-zero status
     wall_s: float = 0.0
     failed: int = 0   # requests retired with a non-zero status (non-finite state, or stalled)
     stalled: int = 0  # of those, retired for exceeding the step limit
@@ -191,6 +192,7 @@ class ServeStats:
         lat = np.array(self.latencies_ms) if self.latencies_ms else np.array([math.nan])
         return {"requests": len(self.latencies_ms), "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "cell_updates_per_s": self.cell_updates / max(self.wall_s, 1e-9),
+                "failed_cell_updates_per_s": self.failed_cell_updates / max(self.wall_s, 1e-9),
                 "wall_s": self.wall_s, "failed": self.failed, "stalled": self.stalled, "max_active": self.max_active}
 
 
@@ -317,7 +319,10 @@ class Server:
                         stats.failed += 1
                     if r.status & 4:
                         stats.stalled += 1
-                    stats.cell_updates += r.cells * r.steps
+                    if r.status:
+                        stats.failed_cell_updates += r.cells * r.steps
+                    else:
+                        stats.cell_updates += r.cells * r.steps
                     stats.latencies_ms.append(1e3 * (r.finished - r.arrival))
                     if self.keep_results:
                         with torch.cuda.stream(self.streams[cls]):

@@ -45,7 +45,7 @@ class RunConfig:
     viscosity: bool = False  # PPM artificial viscosity (schemes/ppm.py:138-170; not run by the reference)
 
     def to_c(self):
-        if self.solver not in C.SOLVER or self.solver == "lw":
+        if self.solver not in C.SOLVER:
             raise C.ConfigError(f"solver {self.solver!r} is not provided by the CUDA library")
         if self.magnetic_2d and self.integrator not in ("euler", "ssprk22", "ssprk33", "ssprk43"):
             raise C.ConfigError("constrained transport runs with Euler and SSP-RK (2,2), (3,3), (4,3)")
@@ -231,6 +231,21 @@ class Solver:
                                          ctypes.c_void_p(f0.data_ptr()),
                                          ctypes.c_void_p(f1.data_ptr() if f1 is not None else 0), eig, _stream()))
         return (f0, f1), (eig[0], eig[1])
+
+    def space_ct(self, order=0):
+        """evolve_space of a constrained-transport grid: fluxes, eigmax, each sweep's face
+        values (2, 8, n0, n1) and the corner field E_z (n0, n1), physical layout."""
+        cfg = self.cfg
+        f0 = torch.empty((self.nv, cfg.n0 + 1, cfg.n1), dtype=cfg.dtype, device=self.device)
+        f1 = torch.empty((self.nv, cfg.n1 + 1, cfg.n0), dtype=cfg.dtype, device=self.device)
+        faces = torch.empty((2, 8, cfg.n0, cfg.n1), dtype=cfg.dtype, device=self.device)
+        corner = torch.empty((cfg.n0, cfg.n1), dtype=cfg.dtype, device=self.device)
+        eig = (ctypes.c_double * 2)()
+        vp = ctypes.c_void_p
+        _lib.check(self.lib.astrea_space_ct(self.handle, vp(self.state.data_ptr()), int(order), vp(f0.data_ptr()),
+                                            vp(f1.data_ptr()), eig, vp(faces[0].data_ptr()), vp(faces[1].data_ptr()),
+                                            vp(corner.data_ptr()), _stream()))
+        return (f0, f1), (eig[0], eig[1]), faces, corner
 
     def time(self, dt, order=0):
         """evolve_time with the given dt, in place on the state."""

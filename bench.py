@@ -285,20 +285,25 @@ def reference_arm(args):
     return 0
 
 
+def batched_cfg(n, ppm, precision=32):
+    """One grid of the batched workload: n^2 four-quadrant data, PPM+HLLC or PLM+LLF, to t=0.25."""
+    from astrea_gb300.solver import RunConfig
+    return RunConfig(dim=2, n0=n, n1=n, model=4, precision=precision, scheme="ppm" if ppm else "plm",
+                     solver="hllc" if ppm else "llf", integrator="ssprk33", boundary="edge", gamma=1.4,
+                     dx=1.0 / n, cfl=0.8, t_end=0.25, compat=False)
+
+
 def batched_leg(steps, warmup, ngrids=512, seed=SEED):
     """512 four-quadrant Riemann grids, sides 2^k (k in 7..10), PLM+LLF / PPM+HLLC 50/50, FP32."""
     import torch
     from astrea_gb300.batch import Batch
-    from astrea_gb300.solver import RunConfig
     from astrea_gb300.serving import Request
     rng = np.random.default_rng(seed)
     cfgs, seeds = [], []
     for g in range(ngrids):
         n = 2 ** int(rng.integers(7, 11))
         ppm = bool(rng.uniform() < .5)
-        cfgs.append(RunConfig(dim=2, n0=n, n1=n, model=4, precision=32, scheme="ppm" if ppm else "plm",
-                              solver="hllc" if ppm else "llf", integrator="ssprk33", boundary="edge", gamma=1.4,
-                              dx=1.0 / n, cfl=0.8, t_end=0.25, compat=False))
+        cfgs.append(batched_cfg(n, ppm))
         seeds.append(int(rng.integers(1 << 31)))
     b = Batch(cfgs)
     for g, c in enumerate(cfgs):
@@ -458,6 +463,180 @@ def mhd_leg(n, steps):
             "status": [int(res[32]["clock"]["status"]), int(res[64]["clock"]["status"])]}
 
 
+def advance_to(s, t_target, chunk=0.5):
+    """Step solver ``s`` until its clock reaches ``t_target``, a checkpoint of its configuration
+    (the step that would cross a checkpoint is clipped to land on it, astrea.py:74-78, so the
+    clock stops exactly there).  Steps go in chunks of ``chunk`` x the steps estimated to remain,
+    so that a chunk never runs past the target.  Returns the clock."""
+    while True:
+        c = s.clock()
+        if c["status"]:
+            raise RuntimeError(f"grid stopped (status {c['status']}) at t={c['t']}")
+        if c["t"] >= t_target * (1 - 1e-12) or c["done"]:
+            return c
+        left = (t_target - c["t"]) / c["dt"] if c["dt"] > 0 else 1.0
+        s.step(max(1, int(left * chunk)), graph=True)
+
+
+def l1_series(make, w, times, twin_ulps=False, t_end=None, checkpoints=None):
+    """L1 of density, FP32 against FP64, at each of ``times`` (checkpoints of the configurations).
+
+    ``make(precision, t_end, checkpoints)`` gives the RunConfig.  With ``twin_ulps`` a second FP64
+    run starts from the same state with every cell's density moved by one unit in the last place
+    (up or down, seeded), which measures how far the flow itself separates two runs that differ
+    only by round-off.  Returns per time: t, L1(rho) FP32-FP64, [L1(rho) FP64-FP64'], step counts,
+    and the wall seconds of each leg."""
+    import torch
+    from astrea_gb300.solver import Solver
+    runs = {"fp32": 32, "fp64": 64}
+    if twin_ulps:
+        runs["fp64_twin"] = 64
+    solvers, wall = {}, {k: 0.0 for k in runs}
+    for k, prec in runs.items():
+        s = Solver(make(prec, t_end, checkpoints))
+        s.initialise(w)
+        if k == "fp64_twin":
+            g = torch.Generator(device="cpu").manual_seed(SEED)
+            up = (torch.rand(s.state[0].shape, generator=g) < .5).to(s.state.device)
+            rho = s.state[0]
+            s.state[0] = torch.where(up, torch.nextafter(rho, torch.full_like(rho, float("inf"))),
+                                     torch.nextafter(rho, torch.full_like(rho, -float("inf"))))
+        s.reset_clock()
+        solvers[k] = s
+    out = []
+    for t in times:
+        row = {"t": t}
+        try:
+            for k, s in solvers.items():
+                t0 = time.perf_counter()
+                c = advance_to(s, t)
+                torch.cuda.synchronize()
+                wall[k] += time.perf_counter() - t0
+                row[f"steps_{k}"] = c["steps"]
+                row[f"t_{k}"] = c["t"]
+        except RuntimeError as e:  # a grid stopped (non-finite): keep the rows so far
+            row["error"] = f"{k}: {e}"
+            out.append(row)
+            break
+        rho64 = solvers["fp64"].state[0]
+        row["l1_rho_fp32_vs_fp64"] = float(torch.mean(torch.abs(solvers["fp32"].state[0].double() - rho64)))
+        if twin_ulps:
+            row["l1_rho_fp64_vs_fp64_ulp_twin"] = float(torch.mean(torch.abs(solvers["fp64_twin"].state[0] - rho64)))
+        row["finite"] = bool(all(torch.isfinite(s.state).all() for s in solvers.values()))
+        out.append(row)
+    del solvers
+    torch.cuda.empty_cache()
+    return {"series": out, "wall_s": wall}
+
+
+def accuracy_shear(n, times, twin_ulps=False):
+    """Configuration 2's error measure (L1(rho), FP32 against FP64) at checkpoints up to its end time."""
+    w = shear_layer(n)
+
+    def make(prec, t_end, checkpoints):
+        from dataclasses import replace
+        return replace(run_config(n, prec), t_end=t_end, checkpoints=checkpoints)
+    res = l1_series(make, w, times, twin_ulps, t_end=1.0, checkpoints=20)
+    res.update({"workload": f"shear layer {n}^2 (the headline method), checkpoints every 0.05 up to t_end=1.0",
+                "twin": "FP64 from the same state with every cell's density moved by +-1 ulp (seeded)"
+                        if twin_ulps else None})
+    return res
+
+
+def accuracy_mhd(n, times):
+    """Configuration 3 (Orszag-Tang, WENO5 + HLLD, CFL 0.4): L1(rho) FP32 against FP64 and div B
+    of both, at checkpoints up to t_end=0.5."""
+    import torch
+    from astrea_gb300.solver import RunConfig, Solver
+    w = orszag_tang(n)
+
+    def make(prec, t_end, checkpoints):
+        return RunConfig(dim=2, n0=n, n1=n, model=8, precision=prec, scheme="weno5", solver="hlld",
+                         integrator="ssprk33", boundary="wrap", gamma=5.0 / 3.0, dx=1.0 / n, cfl=0.4, t_end=t_end,
+                         checkpoints=checkpoints, compat=False)
+    res = l1_series(make, w, times, t_end=0.5, checkpoints=10)
+    res["workload"] = (f"Orszag-Tang {n}^2, WENO5 + HLLD (published form) + SSPRK3, CFL 0.4, cell-centred B, "
+                       f"checkpoints every 0.05 up to t_end=0.5")
+    return res
+
+
+def accuracy_batched(ngrids=512, seed=SEED, fp64_large=(16, 8)):
+    """Configuration 4 to its end time (t=0.25): the whole batch in FP32 until every grid is done
+    (whole-job cell-updates/s), then per-instance L1(rho) against the batched FP64 engine for every
+    128^2 and 256^2 instance and the first ``fp64_large`` (512^2, 1024^2) instances."""
+    import torch
+    from dataclasses import replace
+    from astrea_gb300.batch import Batch
+    from astrea_gb300.serving import Request
+    rng = np.random.default_rng(seed)
+    cfgs, seeds = [], []
+    for g in range(ngrids):
+        nn = 2 ** int(rng.integers(7, 11))
+        ppm = bool(rng.uniform() < .5)
+        cfgs.append(batched_cfg(nn, ppm))
+        seeds.append(int(rng.integers(1 << 31)))
+
+    def fill(b, sub, idx):
+        for g, c in enumerate(sub):
+            r = Request(rid=g, arrival=0.0, dim=2, n=4, mhd=False, scheme="plm", solver="llf", t_end=.25,
+                        seed=seeds[idx[g]])
+            q4 = torch.as_tensor(r.initial_state(), dtype=torch.float64, device="cuda")
+            w = q4[[0, 2]][:, [0, 2]].repeat_interleave(c.n0 // 2, 0).repeat_interleave(c.n1 // 2, 1)
+            b.initialise_one(g, w)
+        torch.cuda.synchronize()
+
+    b = Batch(cfgs)
+    fill(b, cfgs, list(range(ngrids)))
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    clk = b.run(check_every=32)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    wall32 = time.perf_counter() - t0
+    updates = float(sum(int(clk["steps"][g]) * cfgs[g].n0 * cfgs[g].n1 for g in range(ngrids)))
+    rho32 = {g: b.planes(g)[0].double().clone() for g in range(ngrids)}
+    st32 = clk["status"].copy()
+    del b
+    torch.cuda.empty_cache()
+    # FP64 reference instances
+    picked = [g for g in range(ngrids) if cfgs[g].n0 <= 256]
+    for side, count in zip((512, 1024), fp64_large):
+        picked += [g for g in range(ngrids) if cfgs[g].n0 == side][:count]
+    sub = [replace(cfgs[g], precision=64) for g in picked]
+    b64 = Batch(sub)
+    fill(b64, sub, picked)
+    t1 = time.perf_counter()
+    clk64 = b64.run(check_every=32)
+    wall64 = time.perf_counter() - t1
+    per = []
+    for j, g in enumerate(picked):
+        ok = st32[g] == 0 and clk64["status"][j] == 0
+        l1 = float(torch.mean(torch.abs(rho32[g] - b64.planes(j)[0]))) if ok else None
+        per.append({"grid": g, "n": cfgs[g].n0, "scheme": cfgs[g].scheme, "l1_rho": l1,
+                    "status32": int(st32[g]), "status64": int(clk64["status"][j])})
+    del b64
+    torch.cuda.empty_cache()
+    l1s = [p["l1_rho"] for p in per if p["l1_rho"] is not None]
+    by_n = {}
+    for p in per:
+        if p["l1_rho"] is not None:
+            by_n.setdefault(p["n"], []).append(p["l1_rho"])
+    return {"workload": "512 four-quadrant Riemann grids 128^2..1024^2, PLM+LLF/PPM+HLLC 50/50, FP32, to t=0.25",
+            "fp32": {"value": updates / (ms / 1e3), "unit": "cell-updates/s", "ms": ms, "wall_s": wall32,
+                     "cell_updates": updates, "max_steps": int(clk["steps"].max()),
+                     "non_finite_grids": int((st32 != 0).sum()), "t_min": float(clk["t"].min())},
+            "fp64_check": {"instances": len(picked), "finite_in_both": len(l1s), "wall_s": wall64,
+                           "l1_rho_median": float(np.median(l1s)) if l1s else None,
+                           "l1_rho_p90": float(np.percentile(l1s, 90)) if l1s else None,
+                           "l1_rho_max": float(np.max(l1s)) if l1s else None,
+                           "l1_rho_median_by_side": {str(k): float(np.median(v)) for k, v in sorted(by_n.items())},
+                           "non_finite_fp64": int(sum(1 for p in per if p["status64"] != 0)),
+                           "non_finite_fp32_only": int(sum(1 for p in per if p["status32"] != 0 and p["status64"] == 0))},
+            "per_instance": per}
+
+
 def sod_cfg(n):
     from astrea_gb300.solver import RunConfig
     return RunConfig(dim=1, n0=n, model=3, precision=64, scheme="plm", solver="llf", integrator="ssprk33",
@@ -565,6 +744,102 @@ def serving_leg(count, rates, seed=SEED, max_wall_s=30.0):
     return head
 
 
+def run_alone(r, precision, max_steps=200000):
+    """One request solved by the single-grid solver to its end time; returns (status, steps, seconds)."""
+    import torch
+    from astrea_gb300.solver import Solver
+    s = Solver(r.config(precision))
+    s.initialise(r.initial_state())
+    s.reset_clock()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    status = 0
+    try:
+        clk = s.run(max_steps=max_steps, check_every=64)
+        status = clk["status"] | (0 if clk["done"] else 4)
+        steps = clk["steps"]
+    except Exception:  # noqa: BLE001 - a non-finite grid raises; its status is what is wanted
+        clk = s.clock()
+        status, steps = clk["status"] or 1, clk["steps"]
+    torch.cuda.synchronize()
+    return int(status), int(steps), time.perf_counter() - t0
+
+
+def serving_full(count, rates, seed=SEED, max_wall_s=1800.0, alone_sample=40, fp64_max_cells=512 * 512):
+    """The serving workload at its configured size range (1D N log-U[256, 65536], 2D side log-U[128, 2048],
+    150 GB budget): per arrival rate p50/p99 latency and cell-updates/s of the requests that finished cleanly;
+    every request that ended non-finite is solved again alone in FP64 (those of at most ``fp64_max_cells``
+    cells) to see whether the method or FP32 fails it; and a sample of requests solved one at a time by the
+    single-grid solver, for the rate of the same work without batching."""
+    import torch
+    from astrea_gb300.serving import Server, make_requests
+    srv = Server(hbm_budget_bytes=150e9, precision=32, max_slots=256, steps_per_poll=8, max_steps=200000)
+    out = {"mix": "40% 1D N log-U[256,65536], 60% 2D side log-U[128,2048], Euler|MHD 50/50, "
+                  "{PLM,PPM,WENO5}x{LLF,HLLC|HLLD}, t_end U[.05,.3], FP32, HBM budget 150 GB",
+           "requests_per_rate": count, "rates": []}
+    for i, rate in enumerate(rates):
+        reqs = make_requests(count, rate, seed=seed + i)
+        stats = srv.serve(reqs, max_wall_s=max_wall_s)
+        row = stats.summary()
+        row["rate_per_s"] = rate
+        row["unfinished"] = len(stats.unfinished)
+        row["offered_cell_updates"] = float(sum(r.cells * r.steps for r in reqs))
+        failed = [r for r in reqs if r.status & 1]
+        rerun = []
+        for r in failed:
+            if r.cells <= fp64_max_cells:
+                st, steps, _ = run_alone(r, 64)
+                rerun.append({"rid": r.rid, "dim": r.dim, "n": r.n, "mhd": r.mhd, "scheme": r.scheme,
+                              "solver": r.solver, "status32": r.status, "status64": st, "steps64": steps})
+                torch.cuda.empty_cache()
+        row["non_finite"] = len(failed)
+        row["non_finite_rerun_fp64"] = len(rerun)
+        row["non_finite_also_in_fp64"] = sum(1 for x in rerun if x["status64"] & 1)
+        row["rerun"] = rerun
+        out["rates"].append(row)
+        print(json.dumps({"serving_rate": row}), flush=True)
+    # the same kind of work one request at a time (no batching): a seeded sample of the stream
+    reqs = make_requests(alone_sample, rates[0], seed=seed + 100)
+    upd, secs = 0.0, 0.0
+    for r in reqs:
+        st, steps, sec = run_alone(r, 32)
+        if st == 0:
+            upd += r.cells * steps
+            secs += sec
+        torch.cuda.empty_cache()
+    out["alone"] = {"requests": alone_sample, "cell_updates_per_s": upd / max(secs, 1e-9),
+                    "note": "the requests that finished cleanly, solved one after another by the single-grid solver "
+                            "(graph steps, clock read every 64 steps)"}
+    return out
+
+
+def accuracy_campaign(args):
+    """Configurations 2-4 to their end times; one JSON line (not a bench line)."""
+    import torch
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    out = {"accuracy": True}
+
+    def leg(name, fn, *a):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn(*a)
+        except Exception as e:  # noqa: BLE001 - reported in the line
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name + "_s"] = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        print(json.dumps({name: out[name]}), flush=True)
+
+    leg("shear_layer", accuracy_shear, args.n, [0.05, 0.1, 0.25, 0.5, 1.0])
+    leg("shear_layer_twin", accuracy_shear, args.twin_n, [0.05, 0.1, 0.25, 0.5, 1.0], True)
+    leg("orszag_tang", accuracy_mhd, args.mhd_n, [0.05, 0.1, 0.2, 0.3, 0.4, 0.5])
+    leg("batched", accuracy_batched)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -586,9 +861,25 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving legs")
     ap.add_argument("--only-fp32", action="store_true",
                     help="time the FP32 path only (no FP64, e2e, batched, serving or CPU legs); for profiler captures")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="only the accuracy campaign: configurations 2-4 run to their end times (FP32 against FP64 "
+                         "at checkpoints; an FP64 ulp-twin of the shear layer; the batch against the FP64 batch); "
+                         "prints one JSON line")
+    ap.add_argument("--twin-n", type=int, default=1024, help="grid of the FP64 ulp-twin of the shear layer")
+    ap.add_argument("--serving-full", action="store_true",
+                    help="only the serving workload at its configured size range (see --serve-requests, "
+                         "--serve-rates); prints one JSON line")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.accuracy:
+        return accuracy_campaign(args)
+    if args.serving_full:
+        import torch
+        torch.cuda.set_device(0)
+        res = serving_full(args.serve_requests, [float(r) for r in args.serve_rates.split(",")])
+        print(json.dumps({"serving_full": res}), flush=True)
+        return 0
 
     import torch
     ws, rank, local = dist_init()

@@ -42,7 +42,13 @@ extern "C" {
 /* enums: the reference's strings are mapped onto these by the caller
  * (see astrea_gb300/config.py, mirroring functions/generic.py:159-286) */
 enum astrea_scheme { ASTREA_PCM = 0, ASTREA_PLM = 1, ASTREA_PPM = 2, ASTREA_WENO3 = 3, ASTREA_WENO5 = 4, ASTREA_WENO7 = 5 };
-enum astrea_solver { ASTREA_LLF = 0, ASTREA_HLLC = 1, ASTREA_HLLD = 2 };
+/* ASTREA_LW: Lax-Wendroff (num_methods/solvers.py:79-88), the LLF form with the
+ * interface coefficient v_n^2 / max|lambda|.  The reference takes its 'sound
+ * speed' as the second unique column of the LAPACK eigenvalue array, which is
+ * the entropy-wave eigenvalue v_n where LAPACK lists it there (e.g. every
+ * interface of a 1D hydro Sod problem) and another eigenvalue elsewhere; this
+ * library always uses v_n. */
+enum astrea_solver { ASTREA_LLF = 0, ASTREA_HLLC = 1, ASTREA_HLLD = 2, ASTREA_LW = 3 };
 enum astrea_integrator { ASTREA_EULER = 0, ASTREA_SSPRK22 = 1, ASTREA_SSPRK33 = 2, ASTREA_SSPRK43 = 3,
                          ASTREA_SSPRK53 = 4, ASTREA_SSPRK54 = 5, ASTREA_SSPRK104 = 6, ASTREA_RK4 = 7 };
 enum astrea_boundary { ASTREA_EDGE = 0, ASTREA_WRAP = 1 };
@@ -159,6 +165,21 @@ int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* d
 int astrea_space(astrea_handle* h, const void* state, int order, void* flux_ax0, void* flux_ax1, double* eigmax,
                  void* stream);
 
+/* evolve_space for 2D MHD with constrained transport (ASTREA_FLAG_CT;
+ * num_methods/evolvers.py:12-34 with its magnetic block :26-32): everything
+ * astrea_space returns, plus what the reference adds to ``fluxes`` for the
+ * magnetic update.  face_ax0 / face_ax1 receive each sweep's face values
+ * (``data[axes]['wF']``: the value at the face i+1/2 along that sweep of
+ * every cell, 8 primitive planes of n0*n1 elements in the physical layout);
+ * corner receives the corner electric field E_z of mag_field.compute_corner
+ * (mag_field.py:125-187), one n0*n1 plane in the physical layout, whose
+ * transposes the reference stores as ``fluxes[axes]['mag_corner']``.  Any
+ * output may be NULL (a NULL face output leaves that sweep's face values in
+ * the handle's own buffer, from which the corner is still formed).
+ * Synchronises ``stream``. */
+int astrea_space_ct(astrea_handle* h, const void* state, int order, void* flux_ax0, void* flux_ax1, double* eigmax,
+                    void* face_ax0, void* face_ax1, void* corner, void* stream);
+
 /* evolve_time (num_methods/evolvers.py:38-206) with a caller-given dt: the
  * full Runge-Kutta step, in place on ``state``.  The stage-0 fluxes are
  * recomputed on the device from ``state`` (they are a pure function of it). */
@@ -191,7 +212,13 @@ int astrea_reduce_conserved(astrea_handle* h, const void* state, double* sums_ho
  *
  * The first call on each device, made with that device current, looks up the
  * array's address (cudaGetSymbolAddress); make that first call before any
- * stream capture begins.  There is one array per device, so calls that overlap
+ * stream capture begins.  CUDA loads a library's kernels and device arrays
+ * into a context lazily, so that first call is also when the array (and the
+ * two kernels) take their place on the device: make it before the device's
+ * memory is exhausted, e.g. at start-up.  The looked-up address is kept for
+ * the life of the process; after cudaDeviceReset (or anything else that
+ * replaces the device's primary context) it is stale, and this entry point
+ * must not be called again in that process.  There is one array per device, so calls that overlap
  * on the same device (from other threads or on other streams) race on it and
  * give wrong sums: serialise them.  Synchronises ``stream``. */
 int astrea_reduce_conserved_static(const void* state, int precision, long long cells, int nv, double* sums_host,

@@ -140,6 +140,21 @@ def sweep(grid, cfg, axis, label):
     loc = fv.max_speed(fv.gather_range(y_cells, -1, n + 2, bc), g, axis, cfg.eig)
     alpha = np.maximum(loc[:-1], loc[1:])
     eigmax = np.max(alpha)
+    if cfg.solver == "lw":
+        # solvers.py:79-88: the coefficient (sound speed)^2 / max|lambda| of each interface average,
+        # paired like LLF's speeds.  'lapack' takes the reference's sound speed, the second unique
+        # column of the whole eigenvalue array (np.unique(..., axis=-1)[..., 1]); 'analytic' the
+        # entropy-wave eigenvalue v_n, which the kernels use
+        y_pad = fv.gather_range(y_cells, -1, n + 2, bc)
+        if cfg.eig == "lapack":
+            with np.errstate(all="ignore"):
+                ch = np.linalg.eigvals(fv.primitive_jacobian(y_pad, g, axis))
+            ss = np.unique(ch, axis=-1)[..., 1]
+            norm = fv.divide(ss ** 2, np.max(np.abs(ch), axis=-1))
+        else:
+            vn = y_pad[..., 1 + axis % 3]
+            norm = fv.divide(vn * vn, loc)
+        lw_coef = np.maximum(norm[:-1], norm[1:])
     wS_right = fv.gather_range(wS, 0, n + 1, bc)
 
     phys = not cfg.compat
@@ -148,6 +163,8 @@ def sweep(grid, cfg, axis, label):
     def solve(wp_, wm_, qp_, qm_, fp_, fm_):
         if cfg.solver == "llf":
             return riemann.llf(alpha, qp_, qm_, fp_, fm_)
+        if cfg.solver == "lw":
+            return riemann.lax_wendroff(lw_coef, qp_, qm_, fp_, fm_)
         if cfg.solver == "hllc":
             return riemann.hllc(lab, g, wp_, wm_, qp_, qm_, fp_, fm_, physical=phys)
         if cfg.solver == "hlld":

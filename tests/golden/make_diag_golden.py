@@ -1,8 +1,8 @@
 """Golden outputs of the reference's diagnostics (functions/analytic.py).
 
-Run in a container where the reference is at /root/reference:
+Run where a checkout of the reference (mervyzr/astrea) is available:
 
-    python tests/golden/make_diag_golden.py
+    python tests/golden/make_diag_golden.py --reference <path>   (or set ASTREA_REFERENCE)
 
 Stores seeded primitive snapshots with the reference's calculate_TV,
 calculate_solution_error (L1, L2 and max norms against the reference's own
@@ -16,12 +16,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from make_golden import load_reference, make_sv  # noqa: E402
+from make_golden import load_reference, make_sv, reference_path  # noqa: E402
 
 
 def main():
-    R = load_reference(os.environ.get("ASTREA_REFERENCE", "/root/reference"))
-    sys.path.insert(0, os.environ.get("ASTREA_REFERENCE", "/root/reference"))
+    R = load_reference(reference_path())
+    sys.path.insert(0, reference_path())
     from functions import analytic  # noqa: E402
     rng = np.random.default_rng(20261203)
     out = {}

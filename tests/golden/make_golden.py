@@ -1,7 +1,8 @@
 #!/usr/bin/env python3
 """Generate golden vectors by running the reference astrea hot path in-process.
 
-Usage:  python tests/golden/make_golden.py [--reference /root/reference]
+Usage:  python tests/golden/make_golden.py --reference <path of a mervyzr/astrea checkout>
+        (or set ASTREA_REFERENCE)
 
 The reference (mervyzr/astrea) is pure Python + NumPy; its CLI needs h5py,
 PyYAML and tinydb, so this script builds the ``sim_variables`` namedtuple
@@ -31,6 +32,16 @@ SEED = 20261203
 
 HLL = ["hllc", "c", "hlld", "d"]
 COMPLETE = ["os", "osher", "solomon", "osher-solomon", "osher solomon", "es", "entropy", "entropy-stable"]
+
+
+def reference_path():
+    """The reference checkout: ``--reference <path>`` on the command line, or $ASTREA_REFERENCE."""
+    if "--reference" in sys.argv[1:-1]:
+        return sys.argv[sys.argv.index("--reference") + 1]
+    path = os.environ.get("ASTREA_REFERENCE")
+    if not path:
+        sys.exit("the reference checkout is needed: pass --reference <path> or set ASTREA_REFERENCE")
+    return path
 
 
 def load_reference(path):
@@ -78,8 +89,18 @@ def quadrant_ic(rng, n, mhd=False):
     return w
 
 
-def run_case(R, name, sv, steps, grid0=None, store_space=True):
-    """Run ``steps`` steps of the reference loop and save inputs/outputs."""
+ONLY = None  # case-name prefixes to generate (None: all)
+
+
+def wanted(name):
+    return ONLY is None or any(name.startswith(p) for p in ONLY)
+
+
+def run_case(R, name, sv, steps, grid0=None, store_space=True, space_steps=2):
+    """Run ``steps`` steps of the reference loop and save inputs/outputs (the fluxes of the
+    first ``space_steps`` steps)."""
+    if not wanted(name):
+        return
     evolvers, constructor = R["evolvers"], R["constructor"]
     grid = constructor.initialise(sv, convert=True) if grid0 is None else sv.convert_primitive(grid0, sv)
     if grid0 is not None:
@@ -89,7 +110,7 @@ def run_case(R, name, sv, steps, grid0=None, store_space=True):
     t, idx = 0.0, 1
     for s in range(steps):
         fluxes = evolvers.evolve_space(grid, sv)
-        if store_space and s < 2:
+        if store_space and s < space_steps:
             for pos, (axes, val) in enumerate(fluxes.items()):
                 out[f"flux_s{s}_p{pos}"] = np.copy(val["flux"])
                 out[f"eigmax_s{s}_p{pos}"] = np.float64(val["eigmax"])
@@ -116,6 +137,8 @@ def run_case(R, name, sv, steps, grid0=None, store_space=True):
 
 def run_full(R, name, sv):
     """Run to t_end (final grid only)."""
+    if not wanted(name):
+        return
     evolvers, constructor = R["evolvers"], R["constructor"]
     grid = constructor.initialise(sv, convert=True)
     q0 = np.copy(grid)
@@ -185,8 +208,14 @@ def unit_cases(R):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("ASTREA_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("ASTREA_REFERENCE"),
+                    help="path of a mervyzr/astrea checkout (default: $ASTREA_REFERENCE)")
+    ap.add_argument("--only", default=None, help="comma-separated case-name prefixes to (re)generate")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("--reference (or ASTREA_REFERENCE) is required")
+    global ONLY
+    ONLY = args.only.split(",") if args.only else None
     np.seterr(all="ignore")
     R = load_reference(args.reference)
     rng = np.random.default_rng(SEED)
@@ -226,7 +255,69 @@ def main():
     for sub, sol in [("weno5", "hlld"), ("plm", "hlld"), ("ppm", "hlld")]:
         sv = make_sv(R, "orszag-tang", 24, 2, sub, sol, "ssprk(3,3)", gamma=5 / 3, magnetic_2d=True, cfl=0.4)
         run_case(R, f"ot2d_{sub}_{sol}", sv, 3)
-    unit_cases(R)
+    multitile_cases(R)
+    # Lax-Wendroff (solvers.py:79-88): its coefficient column and runs (lw_columns.npz)
+    if wanted("lw_columns"):
+        lw_columns(R)
+    if wanted("unit"):
+        unit_cases(R)
+
+
+def lw_columns(R):
+    """The reference's Lax-Wendroff 'sound speed' next to the entropy-wave eigenvalue.
+
+    solvers.py:84 takes ``np.unique(characteristics, axis=-1)[..., 1]``: the second of the
+    eigenvalue *columns* of the whole interface array, sorted lexicographically, so which wave
+    it is depends on the first interface where the candidate columns differ (and on LAPACK's
+    order within each row).  Stored per step of three 1D runs: that column, v_n (the Jacobian's
+    diagonal) and the reference's grid after the step."""
+    fv, constructor, evolvers = R["fv"], R["constructor"], R["evolvers"]
+    out = {}
+    for tag, config, sub, steps in [("sod_plm", "sod", "plm", 4), ("sod_ppm", "sod", "ppm", 4),
+                                    ("sin_plm", "sin", "plm", 2)]:
+        sv = make_sv(R, config, 64, 1, sub, "lw", "ssprk(3,3)")
+        grid = constructor.initialise(sv, convert=True)
+        out[f"{tag}_q0"] = np.copy(grid)
+        for s in range(steps):
+            data = R["plm"].run(grid, sv) if sub == "plm" else R["ppm"].run(grid, sv, author="mc")
+            jac = data[(0, 1)]["Jacobian"]
+            ch, _ = fv.compute_eigen(jac)
+            out[f"{tag}_col_s{s}"] = np.real(np.unique(ch, axis=-1)[..., 1])
+            out[f"{tag}_vn_s{s}"] = np.copy(jac[..., 1, 1])
+            fluxes = evolvers.evolve_space(grid, sv)
+            dt = sv.cfl * min([sv.dx / r["eigmax"] for r in fluxes.values()])
+            grid = evolvers.evolve_time(np.copy(grid), fluxes, dt, sv)
+            out[f"{tag}_q_{s + 1}"] = np.copy(grid)
+        out[f"{tag}_meta"] = np.array(json.dumps(dict(config=config, subgrid=sub, steps=steps, cells=64, dx=sv.dx,
+                                                      gamma=sv.gamma, cfl=sv.cfl, boundary=sv.boundary,
+                                                      t_end=sv.t_end)))
+    np.savez_compressed(os.path.join(HERE, "lw_columns.npz"), **out)
+    print("lw columns:", len(out))
+
+
+def multitile_cases(R):
+    """Grids of several sweep tiles per axis (tiles are 32 cells along the sweep and 8 or 15 rows
+    across it), so that interior tiles, tile seams, shared-stencil strips and bulk-copied boxes are
+    compared with the reference, not only tiles clamped at the grid's edges: 96^2 hydro in edge
+    and wrap, 64^2 constrained-transport MHD.  Three steps each (both axis orders); the fluxes of
+    the first step."""
+    kw = dict(space_steps=1)
+    run_case(R, "mt96_khi_ppm_hllc", make_sv(R, "khi", 96, 2, "ppm", "hllc", "ssprk(3,3)"), 3, **kw)
+    run_case(R, "mt96_khi_weno5_hllc", make_sv(R, "khi", 96, 2, "weno5", "hllc", "ssprk(3,3)"), 3, **kw)
+    run_case(R, "mt96_khi_plm_lf", make_sv(R, "khi", 96, 2, "plm", "lf", "ssprk(3,3)"), 3, **kw)
+    for sub, sol in [("ppm", "hllc"), ("plm", "lf"), ("weno5", "lf")]:
+        name = f"mt96_quad_edge_{sub}_{sol}"
+        sv = make_sv(R, "ll1", 96, 2, sub, sol, "ssprk(3,3)", boundary="edge", t_end=0.25)
+        for draw in range(50):
+            try:
+                run_case(R, name, sv, 3, grid0=quadrant_ic(np.random.default_rng(SEED + draw), 96), **kw)
+                break
+            except np.linalg.LinAlgError:
+                continue
+    sv = make_sv(R, "orszag-tang", 64, 2, "weno5", "hlld", "ssprk(3,3)", gamma=5 / 3, magnetic_2d=True, cfl=0.4)
+    run_case(R, "mt64_ot_weno5_hlld", sv, 3, **kw)
+    sv = make_sv(R, "orszag-tang", 64, 2, "ppm", "hlld", "ssprk(3,3)", gamma=5 / 3, magnetic_2d=True, cfl=0.4)
+    run_case(R, "mt64_ot_ppm_hlld", sv, 3, **kw)
 
 
 if __name__ == "__main__":

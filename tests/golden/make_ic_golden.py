@@ -1,8 +1,8 @@
 """Golden point primitives of the reference's test problems (constructor.initialise).
 
-Run in a container where the reference is at /root/reference:
+Run where a checkout of the reference (mervyzr/astrea) is available:
 
-    python tests/golden/make_ic_golden.py
+    python tests/golden/make_ic_golden.py --reference <path>   (or set ASTREA_REFERENCE)
 
 For each (config, dimension, cells) it builds ``sim_variables`` with the
 reference's own test table (static/tests.py) and calls its
@@ -21,7 +21,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-from make_golden import load_reference, make_sv  # noqa: E402
+from make_golden import load_reference, make_sv, reference_path  # noqa: E402
 
 CASES = [
     ("sod", 1, 64), ("sedov", 1, 64), ("shu-osher", 1, 64), ("sin", 1, 64), ("gauss", 1, 64), ("lin", 1, 64),
@@ -32,7 +32,7 @@ CASES = [
 
 
 def main():
-    R = load_reference(os.environ.get("ASTREA_REFERENCE", "/root/reference"))
+    R = load_reference(reference_path())
     out = {}
     for i, (config, dim, n) in enumerate(CASES):
         sv = make_sv(R, config, n, dim, "plm", "lf", "ssprk(3,3)")

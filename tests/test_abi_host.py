@@ -111,8 +111,12 @@ def test_model_choice_and_layout_round_trip():
 
 
 def test_runconfig_rejects_unprovided_methods():
+    for s in ("os", "osher-solomon", "es", "entropy-stable"):
+        with pytest.raises(C.ConfigError):
+            C.solver_of(s)
     with pytest.raises(C.ConfigError):
-        RunConfig(dim=1, n0=64, solver="lw").to_c()
+        RunConfig(dim=1, n0=64, solver="roe").to_c()
+    assert RunConfig(dim=1, n0=64, solver="lw").to_c().solver == 3  # Lax-Wendroff: ASTREA_LW
     with pytest.raises(C.ConfigError):
         RunConfig(dim=2, n0=64, n1=64, model=8, solver="hlld", integrator="rk4", magnetic_2d=True).to_c()
     # every integrator of the reference is provided without constrained transport

@@ -84,3 +84,36 @@ def test_fp32_headline_conserves_at_full_size():
         assert abs(after[k] - before[k]) <= 1e-6 * abs(before[k]), (k, before[k], after[k])
     del s
     torch.cuda.empty_cache()
+
+
+def test_fp64_headline_workload_matches_oracle_at_full_size():
+    """The bench's own workload (shear layer 2048^2, PPM + flattening + viscosity, textbook HLLC,
+    SSPRK3, CFL 0.8) in FP64 against the oracle's first two steps (tests/golden/fullsize_shear2048.npz,
+    made by make_fullsize_golden.py): dt bit for bit in value to 1e-15, the full rows and columns at
+    the tile seams and shear interfaces to 1e-14 of each variable's largest magnitude, and the
+    compensated plane sums against the correctly rounded sums."""
+    import bench
+    from tests.golden_io import GOLDEN
+    import json
+    import os
+    with np.load(os.path.join(GOLDEN, "fullsize_shear2048.npz")) as z:
+        g = {k: z[k] for k in z.files}
+    meta = json.loads(str(g["meta"]))
+    s = Solver(bench.run_config(N, 64))
+    s.initialise(bench.shear_layer(N))
+    s.reset_clock()
+    for k in range(1, meta["steps"] + 1):
+        s.step(1, graph=False)
+        clk = s.clock()
+        assert clk["status"] == 0
+        assert clk["dt"] == pytest.approx(float(g[f"dt_{k}"]), rel=1e-15, abs=0)
+        q = s.state  # planes rho, m_x, m_y, E == reference variables 0, 1, 2, 4
+        scale = g[f"absmax_{k}"]
+        rows = q[:, meta["rows"], :].permute(1, 2, 0).cpu().numpy()
+        cols = q[:, :, meta["cols"]].permute(1, 2, 0).cpu().numpy()
+        assert np.max(np.abs(rows - g[f"rows_{k}"]) / scale) <= 1e-14
+        assert np.max(np.abs(cols - g[f"cols_{k}"]) / scale) <= 1e-14
+        sums = s.conserved_sums()
+        assert np.all(np.abs(sums - g[f"sums_{k}"]) <= 1e-13 * scale * N * N)
+    del s
+    torch.cuda.empty_cache()

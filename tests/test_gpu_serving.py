@@ -4,11 +4,12 @@ A small mixed stream (1D/2D, Euler/MHD, PLM/PPM/WENO5 x LLF/HLLC/HLLD) is
 served with arrivals spread over time so that requests join and leave the
 batches while others are running; each finished state is compared with the
 same request solved alone by the single-grid solver.  Both paths run the same
-tile code, except that the single-grid 2D high-order sweeps take their cell
-averages from a pre-pass kernel while the batched tiles form them in place: the
-two FP32 builds contract multiply-adds differently, so the bar is FP32
-rounding, not bit equality: mean difference <= 1e-6 and largest <= 1e-4 of the
-state's scale (in FP64 the two paths agree bit for bit, test_gpu_batch.py).
+tile code and take the 2D high-order cell averages from a pre-pass (the
+single-grid one per grid, the batched one over the strips of every grid of a
+batch), but they are separate FP32 builds that contract multiply-adds
+differently and stage through different paths, so the bar is FP32 rounding,
+not bit equality: mean difference <= 1e-6 and largest <= 1e-4 of the state's
+scale (in FP64 the two paths agree bit for bit, test_gpu_batch.py).
 """
 
 import numpy as np

@@ -89,6 +89,21 @@ def test_static_sums_match_the_handle_sums(cfg):
     assert np.all(np.abs(c - ref1) <= 1e-12 * np.maximum(np.abs(ref1), 1.0)), (c, ref1)
 
 
+def test_static_sums_take_no_device_memory_after_the_first_call():
+    """Once the first call has loaded the module, further calls leave the device's free memory unchanged."""
+    lib, fn = _static_fn()
+    x = torch.rand(8, 1 << 16, dtype=torch.float64, device="cuda")
+    first = _sums_static(fn, x, 64, 8)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        again = _sums_static(fn, x, 64, 8)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert np.array_equal(first, again)
+
+
 def test_static_sums_reject_what_the_scratch_cannot_hold():
     lib, fn = _static_fn()
     x = torch.ones(9 * 16, dtype=torch.float64, device="cuda")

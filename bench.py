@@ -466,19 +466,26 @@ def mhd_leg(n, steps):
 def advance_to(s, t_target, chunk=0.5):
     """Step solver ``s`` until its clock reaches ``t_target``, a checkpoint of its configuration
     (the step that would cross a checkpoint is clipped to land on it, astrea.py:74-78, so the
-    clock stops exactly there).  Steps go in chunks of ``chunk`` x the steps estimated to remain,
-    so that a chunk never runs past the target.  Returns the clock."""
+    clock stops exactly there).  Steps go in chunks of ``chunk`` x the steps estimated to remain
+    at the mean dt of the previous chunk (the clock's own dt may be a clipped one), so that a
+    chunk does not run past the target.  Returns the clock."""
+    prev = None
     while True:
         c = s.clock()
         if c["status"]:
             raise RuntimeError(f"grid stopped (status {c['status']}) at t={c['t']}")
         if c["t"] >= t_target * (1 - 1e-12) or c["done"]:
             return c
-        left = (t_target - c["t"]) / c["dt"] if c["dt"] > 0 else 1.0
-        s.step(max(1, int(left * chunk)), graph=True)
+        if prev is not None and c["steps"] > prev["steps"] and c["t"] > prev["t"]:
+            dt = (c["t"] - prev["t"]) / (c["steps"] - prev["steps"])
+            n = max(1, int((t_target - c["t"]) / dt * chunk))
+        else:
+            n = 1
+        prev = c
+        s.step(n, graph=True)
 
 
-def l1_series(make, w, times, twin_ulps=False, t_end=None, checkpoints=None):
+def l1_series(make, w, times, twin_ulps=False, t_end=None, checkpoints=None, extra=None):
     """L1 of density, FP32 against FP64, at each of ``times`` (checkpoints of the configurations).
 
     ``make(precision, t_end, checkpoints)`` gives the RunConfig.  With ``twin_ulps`` a second FP64
@@ -523,6 +530,8 @@ def l1_series(make, w, times, twin_ulps=False, t_end=None, checkpoints=None):
         if twin_ulps:
             row["l1_rho_fp64_vs_fp64_ulp_twin"] = float(torch.mean(torch.abs(solvers["fp64_twin"].state[0] - rho64)))
         row["finite"] = bool(all(torch.isfinite(s.state).all() for s in solvers.values()))
+        if extra is not None:
+            row.update(extra(solvers))
         out.append(row)
     del solvers
     torch.cuda.empty_cache()
@@ -554,16 +563,22 @@ def accuracy_mhd(n, times):
         return RunConfig(dim=2, n0=n, n1=n, model=8, precision=prec, scheme="weno5", solver="hlld",
                          integrator="ssprk33", boundary="wrap", gamma=5.0 / 3.0, dx=1.0 / n, cfl=0.4, t_end=t_end,
                          checkpoints=checkpoints, compat=False)
-    res = l1_series(make, w, times, t_end=0.5, checkpoints=10)
+    def divs(solvers):
+        # div B of both states, and of the FP64 state rounded to FP32: the floor that FP32 storage
+        # alone puts under a central difference (its rounding of B, amplified by 1/(2 dx))
+        s64 = solvers["fp64"].state
+        return {"div_b_fp32": div_b(solvers["fp32"].state, 1.0 / n)[0], "div_b_fp64": div_b(s64, 1.0 / n)[0],
+                "div_b_fp64_rounded_to_fp32": div_b(s64.float(), 1.0 / n)[0]}
+    res = l1_series(make, w, times, t_end=0.5, checkpoints=10, extra=divs)
     res["workload"] = (f"Orszag-Tang {n}^2, WENO5 + HLLD (published form) + SSPRK3, CFL 0.4, cell-centred B, "
                        f"checkpoints every 0.05 up to t_end=0.5")
     return res
 
 
-def accuracy_batched(ngrids=512, seed=SEED, fp64_large=(16, 8)):
+def accuracy_batched(ngrids=512, seed=SEED, fp64_small=256, fp64_large=(16, 8)):
     """Configuration 4 to its end time (t=0.25): the whole batch in FP32 until every grid is done
     (whole-job cell-updates/s), then per-instance L1(rho) against the batched FP64 engine for every
-    128^2 and 256^2 instance and the first ``fp64_large`` (512^2, 1024^2) instances."""
+    instance of at most ``fp64_small``^2 cells and the first ``fp64_large`` (512^2, 1024^2) ones."""
     import torch
     from dataclasses import replace
     from astrea_gb300.batch import Batch
@@ -601,7 +616,7 @@ def accuracy_batched(ngrids=512, seed=SEED, fp64_large=(16, 8)):
     del b
     torch.cuda.empty_cache()
     # FP64 reference instances
-    picked = [g for g in range(ngrids) if cfgs[g].n0 <= 256]
+    picked = [g for g in range(ngrids) if cfgs[g].n0 <= fp64_small]
     for side, count in zip((512, 1024), fp64_large):
         picked += [g for g in range(ngrids) if cfgs[g].n0 == side][:count]
     sub = [replace(cfgs[g], precision=64) for g in picked]
@@ -632,8 +647,13 @@ def accuracy_batched(ngrids=512, seed=SEED, fp64_large=(16, 8)):
                            "l1_rho_p90": float(np.percentile(l1s, 90)) if l1s else None,
                            "l1_rho_max": float(np.max(l1s)) if l1s else None,
                            "l1_rho_median_by_side": {str(k): float(np.median(v)) for k, v in sorted(by_n.items())},
-                           "non_finite_fp64": int(sum(1 for p in per if p["status64"] != 0)),
-                           "non_finite_fp32_only": int(sum(1 for p in per if p["status32"] != 0 and p["status64"] == 0))},
+                           "non_finite_both": int(sum(1 for p in per if p["status32"] != 0 and p["status64"] != 0)),
+                           "non_finite_fp64_only": int(sum(1 for p in per if p["status32"] == 0 and p["status64"] != 0)),
+                           "non_finite_fp32_only": int(sum(1 for p in per if p["status32"] != 0 and p["status64"] == 0)),
+                           "non_finite_by_scheme": {sch: [int(sum(1 for p in per if p["scheme"] == sch and p["status32"])),
+                                                          int(sum(1 for p in per if p["scheme"] == sch and p["status64"])),
+                                                          int(sum(1 for p in per if p["scheme"] == sch))]
+                                                    for sch in ("plm", "ppm")}},
             "per_instance": per}
 
 
@@ -919,24 +939,26 @@ def main():
                                          kernel_ms, launches, ctypes.c_void_p(stream.cuda_stream)))
     torch.cuda.synchronize()
 
-    # roofline of the sweep kernel: algorithmic bytes per launch / mean launch time.
-    # Per stage a pre-pass reads the stage state and writes its cell averages (FP32: one
-    # order for both sweeps, 2*C*s per cell); each sweep reads the cell averages and writes a
-    # divergence (2*C*s), except the second sweep of stages 1-2, which reads the cell averages,
-    # the other divergence, u0 and the stage state and writes the stage result (5*C*s).
-    # C = 4 stored variables, s = 4 bytes.
+    # roofline of the sweep kernel: algorithmic bytes per launch / mean launch time.  The
+    # algorithmic bytes of a cell-update (one SSPRK3 step of one cell) are 8*C*s = 128 B (the
+    # stage reads 1 + 2 + 2 and writes 3 state passes; C = 4 stored variables, s = 4 bytes); a
+    # step is six sweep launches over every cell, so one launch carries 128 B x cells / 6.
+    # (What a launch actually moves is more -- the cell averages in, a divergence or stage
+    # result out, and the viscous strip -- and is reported as ``traffic``.)
     C, sz = 4, 4
-    alg_bytes_step = cells * C * sz * (2 + 2 + (2 + 5) + (2 + 5))
     sweep_launches = max(launches[0], 1)
-    alg_per_launch = alg_bytes_step * args.steps / sweep_launches
+    alg_per_launch = 8 * C * sz * cells / 6.0
     achieved = alg_per_launch / (kernel_ms[0] / sweep_launches / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     step_alg = cells * 8 * C * sz  # 8 state passes per SSPRK3 step: the minimum traffic
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": SWEEP_DRAM_BYTES * cells / SWEEP_DRAM_CELLS,
                 "kernel": "sweep_kernel (every sweep launch of the timed steps)", "peak_source": peak_kind,
-                "alg_bytes_per_launch": alg_per_launch, "step_frac": step_alg * (value / ws) / cells / 1e9 / peak,
-                "note": "ALU/issue-bound stencil: thousands of FP32 ops per cell-update against 128 B",
+                "alg_bytes_per_launch": alg_per_launch,
+                "alg_bytes_per_cell_update": 8 * C * sz,
+                "step_frac": step_alg * (value / ws) / cells / 1e9 / peak,
+                "note": "issue-bound stencil: hundreds of warp instructions per cell-update against 128 B; "
+                        "frac = (128 B x cells / 6) per sweep launch / mean launch time / measured HBM peak",
                 "kernel_timing": "CUDA events around every launch, in a second pass of the same steps right after "
                                  "the timed graph replay"}
     if launches[3]:

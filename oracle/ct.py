@@ -108,17 +108,23 @@ def induction_rates(mag_corners, dx, bc):
     return out
 
 
-def inverse_reconstruct(grid, bc):
+def inverse_reconstruct(grid, bc, centred=False):
     """Face-averaged B back to cell averages (mag_field.inverse_reconstruct, :191-210).
 
-    The 4-point interpolant of faces i-1/2 .. i+5/2 is centred on cell i+1;
-    that offset is the reference's and is kept.
+    Entry i of a face array is the face i+1/2.  The reference's 4-point
+    interpolant of faces i-1/2 .. i+5/2 is centred on cell i+1, which moves B
+    one cell along its own axis at every stage; that offset is kept unless
+    ``centred``, which interpolates faces i-3/2 .. i+3/2 onto cell i (Felker &
+    Stone 2018, eq. 39).
     """
     new = np.copy(grid)
     for axis in (0, 1):
         frame = grid.transpose(PERM[axis])
         fc = avg_to_centre(frame, bc, [1])
-        cc = -1 / 16 * (gather(fc, -1, bc) + gather(fc, 2, bc)) + 9 / 16 * (fc + gather(fc, 1, bc))
+        if centred:
+            cc = -1 / 16 * (gather(fc, -2, bc) + gather(fc, 1, bc)) + 9 / 16 * (gather(fc, -1, bc) + fc)
+        else:
+            cc = -1 / 16 * (gather(fc, -1, bc) + gather(fc, 2, bc)) + 9 / 16 * (fc + gather(fc, 1, bc))
         ca = centre_to_avg(cc, bc, [0, 1])
         new[..., 5 + axis] = ca.transpose(PERM[axis])[..., 5 + axis]
     return new

@@ -35,6 +35,7 @@ class OracleConfig:
     limiter: str = "minmod"      # PLM slope limiter: minmod | superbee
     eig: str = "lapack"          # lapack (as the reference) | analytic (as the kernels)
     compat: bool = True          # reference quirks in HLLC/HLLD (False: physical-axis solvers, not in the reference)
+    ct_centred: bool = False     # constrained transport: face->cell interpolant centred on the cell (not the reference's)
     flatten: bool = False        # PPM flattening (parity unpinned)
     viscosity: bool = False      # PPM artificial viscosity (parity unpinned)
     av_alpha: float = .3
@@ -219,7 +220,7 @@ def evolve_time(grid, fluxes, dt, cfg, order):
     """evolvers.evolve_time (evolvers.py:38-206) for every integrator."""
     L = lambda fl: compute_L(fl, cfg, order)
     es = lambda k: evolve_space(k, cfg, order)
-    refine = (lambda g: ct.inverse_reconstruct(g, cfg.bc)) if cfg.magnetic_2d else (lambda g: g)
+    refine = (lambda g: ct.inverse_reconstruct(g, cfg.bc, centred=cfg.ct_centred)) if cfg.magnetic_2d else (lambda g: g)
 
     L_zero = L(fluxes)
     if cfg.magnetic_2d:

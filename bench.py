@@ -11,7 +11,10 @@ synthetic data; no dataset is involved.
 Legs of the default arm (all numbers in cell-updates/s):
   value        FP32 (FP64 pressure recovery), state resident in HBM
   fp64_plain   the plain all-FP64 path on the same workload
-  l1_rho       L1(rho) of FP32 against FP64 after the same steps
+  l1_rho       L1(rho) of FP32 against FP64 at t=0.05 on the workload's grid
+  accuracy_t_end_1024  the same error measure to t_end=1.0 on a 1024^2 grid, beside an
+               FP64 twin started one ulp away (--accuracy: the 2048^2 run to t=1.0)
+  batched_to_t_end / mhd_accuracy  configurations 4 and 3 against FP64 (to t=0.25, t=0.05)
   e2e          through the C ABI with the state copied host->device and
                device->host (pinned) every step
   batched      512 independent four-quadrant Riemann grids, 128^2..1024^2,
@@ -990,14 +993,8 @@ def main():
     torch.cuda.synchronize()
     ms64 = f0.elapsed_time(f1)
     value64 = cells * args.fp64_steps / (ms64 / 1e3)
-    # L1(rho) of FP32 against FP64 after the same number of steps from the same initial state
-    k = args.fp64_steps + 1
-    a32 = Solver(run_config(n, 32))
-    a32.initialise(w0)
-    a32.reset_clock()
-    a32.step(k)
-    l1 = float(torch.mean(torch.abs(a32.state[0].double() - s64.state[0])).item())
-    del a32, s64
+    del s64
+    torch.cuda.empty_cache()
 
     # ---- end to end through the C ABI with host buffers (pinned): H2D state, one step, D2H state
     host = torch.empty_like(s32.state, device="cpu").pin_memory()
@@ -1031,9 +1028,20 @@ def main():
             torch.cuda.synchronize()
             torch.cuda.empty_cache()
 
-    batched = serving = mhd = sod = sod_state = snaps = None
+    # ---- accuracy: L1(rho) of FP32 against FP64 at checkpoints of the run (the workload's error
+    # measure).  On the workload's grid at t=0.05; to t_end=1.0 on a 1024^2 grid together with an
+    # FP64 twin started one ulp away (the 2048^2 FP64 run to t=1.0 takes 12 minutes:
+    # ``--accuracy`` runs it)
+    accuracy = leg(accuracy_shear, n, [0.05])
+    accuracy_t_end = leg(accuracy_shear, args.twin_n, [0.05, 0.25, 1.0], True) if not args.no_extras else None
+
+    batched = serving = mhd = sod = sod_state = snaps = mhd_acc = batched_t_end = None
     if not args.no_extras:
         batched = leg(batched_leg, args.batch_steps, 2)
+        batched_t_end = leg(accuracy_batched, 512, SEED, 128, (2, 1))
+        if isinstance(batched_t_end, dict):
+            batched_t_end.pop("per_instance", None)
+        mhd_acc = leg(accuracy_mhd, args.mhd_n, [0.05])
         serving = leg(serving_leg, args.serve_requests, [float(r) for r in args.serve_rates.split(",")])
         mhd = leg(mhd_leg, args.mhd_n, args.mhd_steps)
         sod_out = leg(sod_leg, args.sod_n)
@@ -1083,7 +1091,10 @@ def main():
             "fp64_plain": {"value": value64, "unit": "cell-updates/s", "steps": args.fp64_steps,
                            "ms_per_step": ms64 / args.fp64_steps},
             "fp32_over_fp64": value / ws / value64,
-            "l1_rho_fp32_vs_fp64": l1, "l1_after_steps": k,
+            "l1_rho_fp32_vs_fp64": (accuracy.get("series") or [{}])[0].get("l1_rho_fp32_vs_fp64")
+                                   if isinstance(accuracy, dict) else None,
+            "l1_at_t": 0.05,
+            "accuracy": accuracy, "accuracy_t_end_1024": accuracy_t_end,
             "roofline": roofline,
             "alu_roofline": alu_roofline(value / ws, value64, (clocks or {}).get("sm_max_mhz")),
             "kernel_ms": {"sweep": kernel_ms[0], "combine0": kernel_ms[1], "bookkeeping": kernel_ms[2],
@@ -1095,6 +1106,8 @@ def main():
             "batched": batched,
             "serving": serving,
             "mhd_orszag_tang": mhd,
+            "mhd_accuracy": mhd_acc,
+            "batched_to_t_end": batched_t_end,
             "sod_1d": sod,
             "snapshots": snaps,
             "clocks": clocks,

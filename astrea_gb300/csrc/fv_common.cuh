@@ -31,6 +31,9 @@ template <typename T> __device__ __forceinline__ T npmin(T a, T b) { return (a <
 // (the FP32 path is checked against FP64 by error norms, not bit for bit)
 template <> __device__ __forceinline__ float npmax<float>(float a, float b) { return fmaxf(a, b); }
 template <> __device__ __forceinline__ float npmin<float>(float a, float b) { return fminf(a, b); }
+// maximum that keeps a NaN operand in every precision: the wave-speed maxima use it, so that a
+// non-finite cell reaches the clock (and stops the grid) in FP32 as in FP64
+template <typename T> __device__ __forceinline__ T nanmax(T a, T b) { return (a > b || isnan_(a)) ? a : b; }
 // np.sign: -1, 0 (keeps the zero's sign), +1, NaN
 template <typename T> __device__ __forceinline__ T npsign(T a) { return a > T(0) ? T(1) : (a < T(0) ? T(-1) : a); }
 // fv.divide: a/b where b != 0 else 0

@@ -29,6 +29,24 @@
 namespace astrea {
 
 constexpr double C24 = 1.0 / 24.0;
+
+// The 4th-order transverse conversion x0 - (1/24) (xp - 2 x0 + xm) of the reference
+// (fv.py:105-122, 147-153).  FP64 keeps its operation order (bit parity with NumPy); FP32, which
+// is not bit-compared, forms (1 + 1/12) x0 - (1/24)(xp + xm): three instructions instead of four.
+template <typename T> __device__ __forceinline__ T conv24(T x0, T xm, T xp) {
+  if constexpr (Prec<T>::EXACT) return x0 - T(C24) * ((xp - x0) - (x0 - xm));
+  else return T(1.0 + 2.0 * C24) * x0 - T(C24) * (xp + xm);
+}
+// y - (1/24)(xp - 2 x0 + xm) (the same correction applied to another value)
+template <typename T> __device__ __forceinline__ T sub_d2_24(T y, T x0, T xm, T xp) {
+  if constexpr (Prec<T>::EXACT) return y - T(C24) * ((xp - x0) - (x0 - xm));
+  else return (y + T(2.0 * C24) * x0) - T(C24) * (xp + xm);
+}
+// y + (1/24)(xp - 2 x0 + xm)
+template <typename T> __device__ __forceinline__ T add_d2_24(T y, T x0, T xm, T xp) {
+  if constexpr (Prec<T>::EXACT) return y + T(C24) * ((xp - x0) - (x0 - xm));
+  else return (y - T(2.0 * C24) * x0) + T(C24) * (xp + xm);
+}
 constexpr unsigned kTmaFailed = 0xffffffffu;  // a marching CTA's bulk copy timed out
 
 template <typename T> struct SweepArgs {
@@ -245,12 +263,13 @@ template <typename T> __device__ __forceinline__ T combine(int integ, int stage,
 }
 
 // Block maximum in T (converting a float to double is exact and monotone, so the
-// maximum of the floats is the maximum of their doubles), one atomic per CTA.
+// maximum of the floats is the maximum of their doubles), one atomic per CTA; a NaN
+// speed wins (the clock's atomicMax on IEEE bits orders NaN above +inf).
 template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, unsigned long long* dst) {
   __shared__ T red[32];
   T x = v;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x = npmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+  for (int o = 16; o > 0; o >>= 1) x = nanmax(x, __shfl_xor_sync(0xffffffffu, x, o));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) red[wid] = x;
   __syncthreads();
@@ -258,7 +277,7 @@ template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, un
     const int nw = (blockDim.x + 31) >> 5;
     T y = lane < nw ? red[lane] : T(0);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) y = npmax(y, __shfl_xor_sync(0xffffffffu, y, o));
+    for (int o = 16; o > 0; o >>= 1) y = nanmax(y, __shfl_xor_sync(0xffffffffu, y, o));
     if (lane == 0) atomicMax(dst, (unsigned long long)__double_as_longlong((double)y));
   }
 }
@@ -673,11 +692,11 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     // no boundary map on this tile: one thread per strip of K cells shares the stencil work
     constexpr int K = PpmStrip<G::RW, DIM>::K, NS = G::RW / K;
     constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
-    const int HN = H - skipR;  // rows still to compute
-    for (int e = tid; e < NS * HN * NV; e += nth) {
+    for (int e = tid; e < NS * H * NV; e += nth) {
       // strip-major order: a warp's threads sit on consecutive rows (fewer bank conflicts)
-      const int strip = e / (NV * HN), rem = e % (NV * HN);
-      const int s = rem / HN, row = skipR + rem % HN, col0 = strip * K;
+      const int strip = e / (NV * H), rem = e % (NV * H);
+      const int s = rem / H, row = rem % H, col0 = strip * K;
+      if (row < skipR) continue;  // carried over (marching)
       const int vs0 = s0 + G::R_BEG + col0, vt = t0 - G::RT + row;
       const T* wrow = s_w + (s * WH + row + (G::WT - G::RT)) * WW - (s0 + G::W_BEG);
       T* rl = s_R + ((0 * NV + s) * H + row) * W + col0;
@@ -693,10 +712,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     }
   } else {
     constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
-    const int HN = H - skipR;  // rows still to compute
-    for (int e = tid; e < W * HN * NV; e += nth) {
-      const int s = e / (W * HN), rem = e % (W * HN);
-      const int row = skipR + rem / W, col = rem % W;
+    for (int e = tid; e < W * H * NV; e += nth) {
+      const int s = e / (W * H), rem = e % (W * H);
+      const int row = rem / W, col = rem % W;
+      if (row < skipR) continue;  // carried over (marching)
       const int vs = s0 + G::R_BEG + col, vt = t0 - G::RT + row;
       const int rs = rs_(vs), rt = DIM == 2 ? rt_(vt) : 0;
       const T* wrow = s_w + (s * WH + (rt - (t0 - G::WT))) * WW - (s0 + G::W_BEG);
@@ -777,7 +796,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       // unchanged)
       if (a.want_emax && vj >= s0 && vj < s0 + TS && vj < Ns &&
           ((MARCH && LAM_ALL) || (vt >= t0 && vt < t0 + TT && vt < Nt)))
-        lmax = npmax(lmax, lam);
+        lmax = nanmax(lmax, lam);
     }
     if (a.want_emax) block_max_to_clock(lmax, &a.clock->emax[DIM == 1 ? 0 : AX]);
   }
@@ -817,15 +836,19 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       else { loadR(rs_(vk - 1), rm, wm_); loadR(rs_(vk - 1), rp, wp_); }
       T ww[8], qc[8], qm_[8], qp_[8], q0[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) ww[i] = w[i] - T(C24) * ((wp_[i] - w[i]) - (w[i] - wm_[i]));
+      for (int i = 0; i < 8; ++i) ww[i] = conv24<T>(w[i], wm_[i], wp_[i]);
       p2c<M>(w, q0, gm1);
       p2c<M>(wm_, qm_, gm1);
       p2c<M>(wp_, qp_, gm1);
       p2c<M>(ww, tmp, gm1);
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        qc[i] = T(C24) * ((qp_[i] - q0[i]) - (q0[i] - qm_[i]));
-        q[i] = tmp[i] + qc[i];
+        if constexpr (Prec<T>::EXACT) {
+          qc[i] = T(C24) * ((qp_[i] - q0[i]) - (q0[i] - qm_[i]));
+          q[i] = tmp[i] + qc[i];
+        } else {
+          q[i] = add_d2_24<T>(tmp[i], q0[i], qm_[i], qp_[i]);
+        }
       }
     } else {
       p2c<M>(w, q, gm1);
@@ -896,7 +919,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       T cwp[8], cwm[8], cqp[8], cqm[8], cfp[8], cfm[8], Fc[8], wSr[8];
       auto conv = [&](T* out) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) out[i] = x0[i] - T(C24) * ((xp[i] - x0[i]) - (x0[i] - xm[i]));
+        for (int i = 0; i < 8; ++i) out[i] = conv24<T>(x0[i], xm[i], xp[i]);
       };
       loadL(rs_(vk), rt, x0); loadL(rs_(vk), rm, xm); loadL(rs_(vk), rp, xp);
       conv(cwp);
@@ -915,7 +938,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       load_sm<M>(s_Fa, H * W, fr * W + col, x0); load_sm<M>(s_Fa, H * W, frm * W + col, xm); load_sm<M>(s_Fa, H * W, frp * W + col, xp);
       T F[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) F[i] = Fc[i] - T(C24) * ((xp[i] - x0[i]) - (x0[i] - xm[i]));
+      for (int i = 0; i < 8; ++i) F[i] = sub_d2_24<T>(Fc[i], x0[i], xm[i], xp[i]);
       if constexpr (SCH == PPM) {
         // the viscous flux of this interface sits where F goes: read it, then overwrite
         if (a.viscosity) {

@@ -616,6 +616,11 @@ def accuracy_batched(ngrids=512, seed=SEED, fp64_small=256, fp64_large=(16, 8)):
     updates = float(sum(int(clk["steps"][g]) * cfgs[g].n0 * cfgs[g].n1 for g in range(ngrids)))
     rho32 = {g: b.planes(g)[0].double().clone() for g in range(ngrids)}
     st32 = clk["status"].copy()
+    # the FP32 wave-speed maximum drops a NaN operand, so a grid can hold non-finite cells with a
+    # clean status: such grids count as non-finite too (status bit 0 set here)
+    for g in range(ngrids):
+        if st32[g] == 0 and not bool(torch.isfinite(b.planes(g)).all()):
+            st32[g] |= 1
     del b
     torch.cuda.empty_cache()
     # FP64 reference instances

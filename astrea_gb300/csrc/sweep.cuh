@@ -47,7 +47,6 @@ template <typename T> __device__ __forceinline__ T add_d2_24(T y, T x0, T xm, T 
   if constexpr (Prec<T>::EXACT) return y + T(C24) * ((xp - x0) - (x0 - xm));
   else return (y - T(2.0 * C24) * x0) + T(C24) * (xp + xm);
 }
-constexpr unsigned kTmaFailed = 0xffffffffu;  // a marching CTA's bulk copy timed out
 
 template <typename T> struct SweepArgs {
   const T* q;         // stage input state, NV planes
@@ -208,29 +207,6 @@ template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Sm
   static constexpr int total = total0 + (QS_IN_GAP ? 0 : n_qs);
 };
 
-// Shared memory of a marching CTA (2D high-order tiles that stage wS): the per-tile layout plus a
-// buffer for the face-level rows carried to the next tile (the flattening coefficients and the
-// viscous strip reuse the face region before the face level is formed, so the carried face rows
-// wait outside it), and the bulk-copy stage placed in region 0 after those coefficients and the
-// strip (the per-tile kernel stages in the R region, whose leading rows a marching tile keeps).
-template <typename T, int SCH, int TS, int TT, int NV> struct MarchSmem {
-  using S = Smem<SCH, 2, TS, TT, NV, true>;
-  using G = Geom<SCH, 2, TS, TT>;
-  static constexpr int A = 16 / (int)sizeof(T);
-  // TmaBox of either axis (the same expressions as TmaBox's BW/BH)
-  static constexpr int BW1 = ceil_to(TS + G::W_END - floor_to(G::W_BEG, A), A), BH1 = G::WH;
-  static constexpr int BW0 = TT % A != 0 ? ceil_to(G::WH + A - 1, A) : ceil_to(TT + G::WT - floor_to(-G::WT, A), A);
-  static constexpr int BH0 = G::WW;
-  static constexpr int n_box = NV * (BW1 * BH1 > BW0 * BH0 ? BW1 * BH1 : BW0 * BH0);
-  static constexpr int gap_end = S::QS_IN_GAP ? S::QS_OFF + S::n_qs : (S::ETA_IN_GAP ? S::CB_OFF + S::n_cb : 0);
-  static constexpr int STAGE_OFF = gap_end;  // aligned to 128 bytes at run time (+ up to 128 bytes)
-  static_assert(STAGE_OFF + n_box + 128 / (int)sizeof(T) <= S::n_region0, "the stage does not fit region 0");
-  static constexpr int n_carry_face = 5 * NV * (2 * G::FT) * G::KW;
-  static constexpr int n_carry_lam = (2 * G::FT) * G::YW;
-  static constexpr int CARRY_OFF = S::total;
-  static constexpr int total = S::total + n_carry_face + n_carry_lam;
-};
-
 template <class M, typename T> __device__ __forceinline__ void load_sm(const T* base, int stride, int idx, T* x) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) x[i] = T(0);
@@ -287,22 +263,15 @@ template <typename T> __device__ __forceinline__ void block_max_to_clock(T v, un
 // persistent kernel (a work list of tiles of many grids).  WSIN: the tile
 // stages the precomputed cell-averaged primitives a.ws instead of forming them
 // from the state (2D high-order schemes, single-grid kernel).
-// MARCH (2D, single-grid marching kernel): the bulk copies land in their own region, and with
-// ``cont`` the tile continues the one above it in the same column: the first 2*RT rows of the R
-// level (and of flattening) and the first 2*FT rows of the face level (and of LLF's speeds) are
-// already in place, carried over from that tile, and are not computed again.  ``tma_uses``
-// counts this CTA's bulk-copy waits (the mbarrier's phase).
 template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, bool CL, int NT, bool TMA = false,
-          bool WSIN = false, bool MARCH = false>
+          bool WSIN = false>
 __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int s0, const int t0,
-                                                unsigned char* __restrict__ smem_raw, const bool cont = false,
-                                                unsigned* tma_uses = nullptr) {
+                                                unsigned char* __restrict__ smem_raw) {
   using M = Model<MID>;
   using G = Geom<SCH, DIM, TS, TT>;
   using S = Smem<SCH, DIM, TS, TT, M::NV, WSIN>;
   static_assert(!WSIN || (DIM == 2 && G::HO), "precomputed wS is for 2D high-order tiles");
   static_assert(!TMA || WSIN || !G::HO, "the TMA box holds the wS level: high-order tiles stage it precomputed");
-  static_assert(!MARCH || (WSIN && DIM == 2 && MID != 8), "marching tiles: 2D Euler tiles that stage wS");
   constexpr int NV = M::NV;
   T* sm = reinterpret_cast<T*>(smem_raw);
   T* s_q = sm;                       // region 0 (a): q and its point primitives
@@ -312,22 +281,6 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   T* s_w = sm + S::n_region0;
   T* s_R = s_w + S::n_w;
   T* s_lam = s_R + S::n_R;
-  // rows already in place (carried over from the tile above in a marching CTA)
-  const int skipR = (MARCH && cont) ? 2 * G::RT : 0;
-  const int skipF = (MARCH && cont) ? 2 * G::FT : 0;
-  // the bulk-copy stage: the (still unused) R region, or the marching kernel's own region
-  auto stage_area = [&]() -> T* {
-    if constexpr (MARCH) {
-      using MS = MarchSmem<T, SCH, TS, TT, M::NV>;
-      return reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(sm + MS::STAGE_OFF) + 127) & ~uintptr_t(127));
-    } else {
-      return reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_R) + 127) & ~uintptr_t(127));
-    }
-  };
-  // mbarrier set-up once per CTA; the phase to wait for is the parity of the CTA's waits so far
-  auto bar_phase = [&]() -> unsigned { return (MARCH && tma_uses) ? (*tma_uses & 1u) : 0u; };
-  auto bar_first = [&]() -> bool { return !(MARCH && tma_uses) || *tma_uses == 0; };
-  auto bar_used = [&]() { if (MARCH && tma_uses) *tma_uses += 1; };
 
   const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
   const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
@@ -405,12 +358,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       using B = TmaBox<T, SCH, DIM, AX, TS, TT, NV>;
       using SB = StripBox<T, AX, TS, TT>;
       __shared__ unsigned long long s_bar;
-      T* stage = stage_area();
+      T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_R) + 127) & ~uintptr_t(127));
       if (tid == 0) {
-        if (bar_first()) {
-          mbar_init(&s_bar, 1);
-          mbar_fence_init();
-        }
+        mbar_init(&s_bar, 1);
+        mbar_fence_init();
         unsigned bytes = (unsigned)B::BYTES;
         if (strip_tma) bytes += (unsigned)(NV * SB::BH * SB::BW * (int)sizeof(T));
         mbar_arrive_expect_tx(&s_bar, bytes);
@@ -421,18 +372,15 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       }
       __syncthreads();  // the barrier is initialised before anyone waits on it
       if (!strip_tma) stage_strip();
-      const unsigned phase = bar_phase();
-      const bool landed = mbar_wait_timed(&s_bar, phase, kCopyWaitNs);
+      const bool landed = mbar_wait_timed(&s_bar, 0, kCopyWaitNs);
       if (!__syncthreads_and(landed)) {
         // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
         if (tid == 0) {
           atomicOr(&a.clock->status, 2);
-          mbar_wait_timed(&s_bar, phase, kDrainWaitNs);
+          mbar_wait_timed(&s_bar, 0, kDrainWaitNs);
         }
-        if (MARCH && tma_uses) *tma_uses = kTmaFailed;  // the marching CTA stops
         return;
       }
-      bar_used();
       const int xo = B::xoff(t0);
       for (int e = tid; e < W * H; e += nth) {
         int row, col;
@@ -457,30 +405,25 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     // one thread issues the bulk copy of the whole box into the (still unused) R region
     using B = TmaBox<T, SCH, DIM, AX, TS, TT, NV>;
     __shared__ unsigned long long s_bar;
-    T* stage = stage_area();
+    T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_R) + 127) & ~uintptr_t(127));
     if (tid == 0) {
-      if (bar_first()) {
-        mbar_init(&s_bar, 1);
-        mbar_fence_init();
-      }
+      mbar_init(&s_bar, 1);
+      mbar_fence_init();
       mbar_arrive_expect_tx(&s_bar, (unsigned)B::BYTES);
       const CUtensorMap* map = a.tmaps + (AX * 2 + B::TILE_ID);
       if (AX == 1) tma_load_3d(stage, map, B::x0(s0, t0), t0 - G::QT, 0, &s_bar);
       else tma_load_3d(stage, map, B::x0(s0, t0), s0 + G::Q_BEG, 0, &s_bar);
     }
     __syncthreads();  // the barrier is initialised before anyone waits on it
-    const unsigned phase = bar_phase();
-    const bool landed = mbar_wait_timed(&s_bar, phase, kCopyWaitNs);
+    const bool landed = mbar_wait_timed(&s_bar, 0, kCopyWaitNs);
     if (!__syncthreads_and(landed)) {
       // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
       if (tid == 0) {
         atomicOr(&a.clock->status, 2);
-        mbar_wait_timed(&s_bar, phase, kDrainWaitNs);
+        mbar_wait_timed(&s_bar, 0, kDrainWaitNs);
       }
-      if (MARCH && tma_uses) *tma_uses = kTmaFailed;  // the marching CTA stops
       return;
     }
-    bar_used();
     constexpr int W = G::QW, H = G::QH;
     const int xo = B::xoff(t0);
     for (int e = tid; e < W * H; e += nth) {
@@ -602,7 +545,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         constexpr int CB_BEG = G::R_BEG - 2, E_BEG = G::R_BEG - 1;
         constexpr double DZ = 0.85 - 0.75;
         T* s_cb = sm + S::CB_OFF;
-        for (int e = tid + skipR * CW; e < CW * H; e += nth) {
+        for (int e = tid; e < CW * H; e += nth) {
           const int row = e / CW, col = e % CW;
           const int y = rs_(s0 + CB_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
           auto P = [&](int x) -> T { return wv(PP, x, rt); };
@@ -622,7 +565,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
           s_cb[row * CW + col] = cb;
         }
         __syncthreads();
-        for (int e = tid + skipR * EW; e < EW * H; e += nth) {
+        for (int e = tid; e < EW * H; e += nth) {
           const int row = e / EW, col = e % EW;
           const int x = rs_(s0 + E_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
           const T* cbrow = s_cb + row * CW - (s0 + CB_BEG);
@@ -696,7 +639,6 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       // strip-major order: a warp's threads sit on consecutive rows (fewer bank conflicts)
       const int strip = e / (NV * H), rem = e % (NV * H);
       const int s = rem / H, row = rem % H, col0 = strip * K;
-      if (row < skipR) continue;  // carried over (marching)
       const int vs0 = s0 + G::R_BEG + col0, vt = t0 - G::RT + row;
       const T* wrow = s_w + (s * WH + row + (G::WT - G::RT)) * WW - (s0 + G::W_BEG);
       T* rl = s_R + ((0 * NV + s) * H + row) * W + col0;
@@ -715,7 +657,6 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     for (int e = tid; e < W * H * NV; e += nth) {
       const int s = e / (W * H), rem = e % (W * H);
       const int row = rem / W, col = rem % W;
-      if (row < skipR) continue;  // carried over (marching)
       const int vs = s0 + G::R_BEG + col, vt = t0 - G::RT + row;
       const int rs = rs_(vs), rt = DIM == 2 ? rt_(vt) : 0;
       const T* wrow = s_w + (s * WH + (rt - (t0 - G::WT))) * WW - (s0 + G::W_BEG);
@@ -746,20 +687,6 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     load_sm<M>(s_R + NV * G::RH * G::RW, G::RH * G::RW, (rt - (t0 - G::RT)) * G::RW + (x - (s0 + G::R_BEG)), out);
   };
 
-  // ---- marching: the face rows (and LLF's speeds) this tile shares with the tile above, back from
-  // the carry buffer now that the flattening coefficients and the viscous strip are dead
-  if constexpr (MARCH) {
-    if (cont) {
-      using MS = MarchSmem<T, SCH, TS, TT, NV>;
-      const T* carry = sm + MS::CARRY_OFF;
-      constexpr int nF = 5 * NV * (2 * G::FT) * G::KW, nL = SOL == LLF ? (2 * G::FT) * G::YW : 0;
-      for (int e = tid; e < nF + nL; e += nth) {
-        if (e < nF) s_fa[(e / (2 * G::FT * G::KW)) * G::FH * G::KW + e % (2 * G::FT * G::KW)] = carry[e];
-        else s_lam[e - nF] = carry[MS::n_carry_face + (e - nF)];
-      }
-    }
-  }
-
   // ---- level lambda: wave speed of the interface average right of each cell (fv.compute_eigen)
   // LLF reads the speeds on both sides of every interface of the face levels; the
   // HLL-type solvers use them only for the tile maximum (the time step), so they
@@ -768,9 +695,8 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   if (LAM_ALL || a.want_emax) {
     constexpr int W = LAM_ALL ? G::YW : TS, H = LAM_ALL ? G::FH : TT;
     constexpr int C_OFF = LAM_ALL ? 0 : 1, R_OFF = LAM_ALL ? 0 : G::FT;
-    const int skipL = LAM_ALL ? skipF : 0;  // LLF's speeds of the carried face rows are in place
     T lmax = T(0);
-    for (int e = tid + skipL * W; e < W * H; e += nth) {
+    for (int e = tid; e < W * H; e += nth) {
       const int row = e / W + R_OFF, col = e % W + C_OFF;
       const int vj = s0 - 1 + col, vt = t0 - G::FT + row;
       const int rj = rs_(vj), rt = DIM == 2 ? rt_(vt) : 0;
@@ -791,12 +717,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         const T vn = y[1 + (DIM == 1 ? 0 : AX)];
         s_lam[row * G::YW + col] = a.lw ? dvd(vn * vn, lam) : lam;
       }
-      // (a marching CTA's LLF tile counts its halo rows too: an own row it does not recompute was
-      // a halo row of the tile above, and every row it counts is a real cell's, so the maximum is
-      // unchanged)
-      if (a.want_emax && vj >= s0 && vj < s0 + TS && vj < Ns &&
-          ((MARCH && LAM_ALL) || (vt >= t0 && vt < t0 + TT && vt < Nt)))
-        lmax = nanmax(lmax, lam);
+      if (a.want_emax && vj >= s0 && vj < s0 + TS && vj < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) lmax = nanmax(lmax, lam);
     }
     if (a.want_emax) block_max_to_clock(lmax, &a.clock->emax[DIM == 1 ? 0 : AX]);
   }
@@ -886,7 +807,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     T* s_fm = s_fa + 3 * NV * H * W;
     T* s_Fa = s_fa + 4 * NV * H * W;
     // items with the R level's row pitch (conflict-free loads across a row change)
-    for (int e = tid + skipF * G::RW; e < G::RW * H; e += nth) {
+    for (int e = tid; e < G::RW * H; e += nth) {
       const int row = e / G::RW, col = e % G::RW;
       if (col >= W) continue;
       const int vk = s0 + col, vt = t0 - G::FT + row;
@@ -992,32 +913,6 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       }
     }
   }
-
-  // ---- marching: keep the rows the next tile of the column shares with this one.  R rows
-  // [TT, TT + 2*RT) move to [0, 2*RT) in place (nothing touches the R level before the next tile's
-  // R level); face rows [TT, TT + 2*FT) and LLF's speeds go to the carry buffer (the next tile's
-  // flattening and viscous strip use the face region first).  No level read here is written by
-  // the divergence step above, so no barrier is needed before this.
-  if constexpr (MARCH) {
-    using MS = MarchSmem<T, SCH, TS, TT, NV>;
-    T* carry = sm + MS::CARRY_OFF;
-    constexpr int nR = 2 * NV * (2 * G::RT) * G::RW;
-    constexpr int nF = 5 * NV * (2 * G::FT) * G::KW, nL = SOL == LLF ? (2 * G::FT) * G::YW : 0;
-    static_assert(TT >= 2 * G::RT, "carried R rows overlap their sources");
-    for (int e = tid; e < nR + nF + nL; e += nth) {
-      if (e < nR) {
-        T* p = s_R + (e / (2 * G::RT * G::RW)) * G::RH * G::RW;
-        const int rem = e % (2 * G::RT * G::RW);
-        p[rem] = p[TT * G::RW + rem];
-      } else if (e < nR + nF) {
-        const int f = e - nR;
-        carry[f] = s_fa[(f / (2 * G::FT * G::KW)) * G::FH * G::KW + TT * G::KW + f % (2 * G::FT * G::KW)];
-      } else {
-        const int l = e - nR - nF;
-        carry[MS::n_carry_face + l] = s_lam[TT * G::YW + l];
-      }
-    }
-  }
 }
 
 // Clamping is only needed on outflow grids, for tiles whose widest level
@@ -1025,21 +920,19 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 // With TMA (single-grid 2D kernels), tiles whose whole TMA box lies inside the
 // grid are staged by the bulk copy; the others load per thread as without it.
 template <typename T, int MID, int SCH, int SOL, int DIM, int AX, int TS, int TT, int NT = (DIM == 1 ? 64 : 256),
-          bool TMA_OK = false, bool WSIN = false, bool MARCH = false>
+          bool TMA_OK = false, bool WSIN = false>
 __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, const int t0,
-                                           unsigned char* __restrict__ smem_raw, const bool cont = false,
-                                           unsigned* tma_uses = nullptr) {
+                                           unsigned char* __restrict__ smem_raw) {
   using G = Geom<SCH, DIM, TS, TT>;
   using S = Smem<SCH, DIM, TS, TT, Model<MID>::NV, WSIN>;
   const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
   const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
   if constexpr (TMA_OK && DIM == 2 && (WSIN || !G::HO)) {
     using B = TmaBox<T, SCH, DIM, AX, TS, TT, Model<MID>::NV>;
-    if constexpr (MARCH || (size_t)S::n_R * sizeof(T) >= (size_t)B::BYTES + 128) {
+    if constexpr ((size_t)S::n_R * sizeof(T) >= (size_t)B::BYTES + 128) {
       const bool box_in = a.tmaps != nullptr && B::inside(s0, t0, a.n0, a.n1);
       if (box_in) {
-        sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, true, WSIN, MARCH>(a, s0, t0, smem_raw, cont,
-                                                                                       tma_uses);
+        sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, true, WSIN>(a, s0, t0, smem_raw);
         return;
       }
     }
@@ -1047,10 +940,8 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
   constexpr int BEG = WSIN ? G::W_BEG : G::Q_BEG, END = WSIN ? G::W_END : G::Q_END, HT = WSIN ? G::WT : G::QT;
   const bool inside = s0 + BEG >= 0 && s0 + TS + END <= Ns && (DIM == 1 || (t0 - HT >= 0 && t0 + TT + HT <= Nt));
   if (a.bc == EDGE && !inside)
-    sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, true, NT, false, WSIN, MARCH>(a, s0, t0, smem_raw, cont,
-                                                                                   tma_uses);
-  else sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, false, WSIN, MARCH>(a, s0, t0, smem_raw, cont,
-                                                                                       tma_uses);
+    sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, true, NT, false, WSIN>(a, s0, t0, smem_raw);
+  else sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, false, WSIN>(a, s0, t0, smem_raw);
 }
 
 // The single-grid kernels of 2D high-order schemes stage the precomputed wS.
@@ -1069,32 +960,6 @@ __global__ void __launch_bounds__(NT, (SweepOcc<T, MID, NT>::value)) sweep_kerne
   extern __shared__ __align__(16) unsigned char smem_raw[];
   sweep_tile<T, MID, SCH, SOL, DIM, AX, TS, TT, NT, true, sweep_wsin<SCH, DIM>()>(a, blockIdx.x * TS, blockIdx.y * TT,
                                                                                smem_raw);
-}
-
-// The marching sweep kernel (2D Euler grids of the single-grid engine): a persistent grid
-// whose CTAs take equal contiguous runs of the tiles in column-major order (down each column of
-// tiles across the sweep, then the next column).  Consecutive tiles of a column share 2*RT rows
-// of the R level and 2*FT rows of the face level, which are carried over instead of recomputed:
-// the transverse halo of every level but the staged one is computed once per column run, not
-// once per tile.  Results are those of sweep_kernel bit for bit (same expressions per element).
-template <typename T, int MID, int SCH, int SOL, int AX, int TS, int TT, int NT>
-__global__ void __launch_bounds__(NT, (SweepOcc<T, MID, NT>::value)) sweep_march_kernel(const SweepArgs<T> a) {
-  if (a.clock->done) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr bool WSIN = sweep_wsin<SCH, 2>();
-  const int Ns = AX == 0 ? a.n0 : a.n1, Nt = AX == 0 ? a.n1 : a.n0;
-  const int nS = (Ns + TS - 1) / TS, nT = (Nt + TT - 1) / TT;
-  const long long total = (long long)nS * nT;
-  const long long beg = total * blockIdx.x / gridDim.x, end = total * (blockIdx.x + 1) / gridDim.x;
-  unsigned tma_uses = 0;
-  for (long long w = beg; w < end; ++w) {
-    const int si = (int)(w / nT), ti = (int)(w % nT);
-    const bool cont = w > beg && ti > 0;
-    sweep_tile<T, MID, SCH, SOL, 2, AX, TS, TT, NT, true, WSIN, true>(a, si * TS, ti * TT, smem_raw, cont,
-                                                                       &tma_uses);
-    if (tma_uses == kTmaFailed) return;
-    __syncthreads();  // every read of this tile's levels is done before the next tile writes them
-  }
 }
 
 }  // namespace astrea

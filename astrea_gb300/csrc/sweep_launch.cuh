@@ -2,8 +2,6 @@
 // Each sweep_<prec>_<scheme>.cu translation unit instantiates get_sweep for one
 // (precision, scheme) pair so the build compiles them in parallel.
 #pragma once
-#include <cstdlib>
-
 #include "sweep.cuh"
 
 namespace astrea {
@@ -17,15 +15,11 @@ template <typename T> using SweepFn = cudaError_t (*)(const SweepArgs<T>&, cudaS
 // Euler tiles only: two CTAs per SM in FP32 at 64 registers, one in FP64 at
 // 122 registers and 182 KB of shared memory, where fewer halo cells per cell
 // matter because the FP64 pipe bounds the kernel).
-// Candidate 2 is the marching kernel with 32 x 15 tiles (2D Euler grids whose high-order
-// schemes stage the pre-pass's cell averages): persistent CTAs walk down columns of tiles and
-// carry the rows consecutive tiles share.
 constexpr int TS1 = 32, NT1 = 64;
-constexpr int NTILES2 = 3;
+constexpr int NTILES2 = 2;
 template <int I> struct Tile2;
 template <> struct Tile2<0> { static constexpr int TS = 32, TT = 8, NT = 256; };
 template <> struct Tile2<1> { static constexpr int TS = 32, TT = 15, NT = 512; };
-template <> struct Tile2<2> { static constexpr int TS = 32, TT = 15, NT = 512; };
 
 template <typename T, int MID, int SCH, int DIM, int TS, int TT> constexpr size_t sweep_smem_bytes() {
   return sizeof(T) * (size_t)Smem<SCH, DIM, TS, TT, Model<MID>::NV, sweep_wsin<SCH, DIM>()>::total;
@@ -53,39 +47,6 @@ cudaError_t launch_sweep(const SweepArgs<T>& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <typename T, int MID, int SCH, int SOL, int AX, int TS, int TT, int NT>
-cudaError_t launch_sweep_march(const SweepArgs<T>& a, cudaStream_t st) {
-  constexpr size_t bytes = sizeof(T) * (size_t)MarchSmem<T, SCH, TS, TT, Model<MID>::NV>::total;
-  static_assert(bytes <= 227 * 1024, "marching tile exceeds the shared memory of one CTA");
-  auto k = sweep_march_kernel<T, MID, SCH, SOL, AX, TS, TT, NT>;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  static unsigned long long configured = 0ull;  // one bit per device
-  static int ctas[64] = {};                     // persistent grid per device: resident CTAs x SMs
-  const unsigned long long bit = 1ull << (dev & 63);
-  if (!(configured & bit)) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, NT, bytes);
-    if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    ctas[dev & 63] = (per_sm > 0 ? per_sm : 1) * sms;
-    configured |= bit;
-  }
-  if (a.n0 <= 0) return cudaSuccess;  // configure-only call (before any graph capture)
-  const int Ns = AX == 0 ? a.n0 : a.n1, Nt = AX == 0 ? a.n1 : a.n0;
-  const long long tiles = (long long)((Ns + TS - 1) / TS) * ((Nt + TT - 1) / TT);
-  int limit = ctas[dev & 63];
-  // ASTREA_MARCH_CTAS=<n> caps the grid (tests: long runs of tiles per CTA on small grids)
-  const char* cap = std::getenv("ASTREA_MARCH_CTAS");
-  if (cap && std::atoi(cap) > 0 && std::atoi(cap) < limit) limit = std::atoi(cap);
-  const int grid = (int)(tiles < limit ? tiles : limit);
-  k<<<grid, NT, bytes, st>>>(a);
-  return cudaGetLastError();
-}
-
 // launcher of one (model, scheme, solver, dimension, axis) for tile candidate ``tile``; nullptr if that
 // tile is not built for it
 template <typename T, int MID, int SCH, int SOL, int DIM, int AX> SweepFn<T> sweep_for_tile(int tile) {
@@ -95,10 +56,6 @@ template <typename T, int MID, int SCH, int SOL, int DIM, int AX> SweepFn<T> swe
     if (tile == 0) return &launch_sweep<T, MID, SCH, SOL, 2, AX, Tile2<0>::TS, Tile2<0>::TT, Tile2<0>::NT>;
     if constexpr (MID != 8) {
       if (tile == 1) return &launch_sweep<T, MID, SCH, SOL, 2, AX, Tile2<1>::TS, Tile2<1>::TT, Tile2<1>::NT>;
-      if constexpr (sweep_wsin<SCH, 2>()) {
-        if (tile == 2)
-          return &launch_sweep_march<T, MID, SCH, SOL, AX, Tile2<2>::TS, Tile2<2>::TT, Tile2<2>::NT>;
-      }
     }
     return nullptr;
   }

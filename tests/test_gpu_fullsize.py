@@ -118,35 +118,3 @@ def test_fp64_headline_workload_matches_oracle_at_full_size():
     del s
     torch.cuda.empty_cache()
 
-
-@pytest.mark.parametrize("precision", [64, 32])
-def test_marching_kernel_equals_per_tile_kernel(precision, monkeypatch):
-    """The marching sweep (tile candidate 2: persistent CTAs that carry the rows consecutive tiles
-    share) against the per-tile sweep with the same 32 x 15 tiles (candidate 1) on the headline
-    workload at 1024^2, where every CTA walks runs of about 15 tiles: FP64 bit for bit (the same
-    expressions per element, compiled without contraction); FP32 to its rounding (the two kernels
-    may contract multiply-adds differently, and a rounding difference can flip a limiter branch
-    near a discontinuity: mean difference <= 1e-6 and largest <= 1e-4 of the state's largest
-    magnitude)."""
-    import bench
-    n = 1024
-    out = {}
-    for tile in (1, 2):
-        monkeypatch.setenv("ASTREA_SWEEP_TILE", str(tile))
-        s = Solver(bench.run_config(n, precision))
-        s.initialise(bench.shear_layer(n))
-        s.reset_clock()
-        s.step(3)
-        assert s.clock()["status"] == 0
-        assert s.sweep_tiles() == [(32, 15), (32, 15)]
-        out[tile] = (s.state.clone(), s.clock())
-        del s
-    (a, ca), (b, cb) = out[1], out[2]
-    if precision == 64:
-        assert torch.equal(a, b)
-        assert ca == cb
-    else:
-        d = (a - b).abs()
-        scale = float(a.abs().max())
-        assert float(d.mean()) <= 1e-6 * scale and float(d.max()) <= 1e-4 * scale
-    torch.cuda.empty_cache()

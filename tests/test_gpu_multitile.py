@@ -4,8 +4,7 @@ The golden cases ``mt*`` (tests/golden/make_golden.py:multitile_cases) are
 96^2 hydro grids (edge and wrap: PPM+HLLC, WENO5+HLLC, PLM+LLF, WENO5+LLF)
 and 64^2 constrained-transport MHD grids (PPM, WENO5 + HLLD) run by the
 reference's own evolve_space / evolve_time.  With sweep tiles of 32 cells
-along the sweep and 8 or 15 rows across (and the marching kernel, which
-carries rows from one tile to the next), these grids have interior tiles
+along the sweep and 8 or 15 rows across, these grids have interior tiles
 (unclamped, shared-stencil PPM strips, bulk-copied staging boxes), tile
 seams along and across the sweep, and ragged last tiles, besides the clamped
 edge tiles.  Each case runs with every tile candidate, with the bulk copies on
@@ -66,15 +65,11 @@ def oracle_runs():
 
 
 @pytest.mark.parametrize("tma", [1, 0])
-@pytest.mark.parametrize("tile", [0, 1, 2])
+@pytest.mark.parametrize("tile", [0, 1])
 @pytest.mark.parametrize("name", MT)
 def test_multitile_steps_match_reference(name, tile, tma, oracle_runs, monkeypatch):
-    """Tile 2 is the marching kernel (high-order Euler grids; the others fall back to tile 0),
-    here with three persistent CTAs, so that each walks runs of 7 or more tiles and crosses from
-    one column of tiles to the next."""
     monkeypatch.setenv("ASTREA_SWEEP_TILE", str(tile))
     monkeypatch.setenv("ASTREA_TMA", str(tma))
-    monkeypatch.setenv("ASTREA_MARCH_CTAS", "3")
     g = golden_io.load(name)
     meta = g["meta"]
     gc, _ = configs(meta, g["q0"])

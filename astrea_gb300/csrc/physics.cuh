@@ -293,8 +293,10 @@ template <typename T> __device__ __forceinline__ T pick3(T x0, T x1, T x2, int i
 // min(uL, uR), star momenta without their density factors, the right Alfven
 // speed's sign, momenta in the energy's v.B) and blows up on the Orszag-Tang
 // vortex.  One normal field for both sides: the mean of the two face states'.
-// A star state whose denominator rho (S - u)(S - S_M) - Bn^2 vanishes
-// (relative 1e-10) keeps its transverse velocity and field.
+// A star state whose denominator rho (S - u)(S - S_M) - Bn^2 vanishes keeps its
+// transverse velocity and field: relative to its terms, below 1e-10 in FP64 and
+// below 1e-5 in FP32, whose round-off alone leaves ~1e-7 of them in the
+// difference (a smaller FP32 threshold divides by that noise).
 template <typename T> struct HlldStar { T rs, vs, ws, bys, bzs, Es, vbs; };
 
 template <typename T>
@@ -329,7 +331,7 @@ __device__ void hlld_textbook(int a, T gamma, const T* wp, const T* wm, const T*
     x.rs = r * dvd(d, s - sM);
     const T rds = (r * d) * (s - sM);
     const T dn = rds - bn2;
-    const bool degen = abs_(dn) <= T(1e-10) * (abs_(rds) + bn2);
+    const bool degen = abs_(dn) <= T(Prec<T>::EXACT ? 1e-10 : 1e-5) * (abs_(rds) + bn2);
     const T g = dvd(sM - u, dn);
     const T fac = dvd((r * d) * d - bn2, dn);
     x.vs = degen ? v : v - (Bn * by) * g;

@@ -17,7 +17,7 @@ EXPORTS = [
     "astrea_reset_clock", "astrea_step", "astrea_graph_step", "astrea_get_clock", "astrea_space", "astrea_time",
     "astrea_to_primitive", "astrea_reduce_conserved", "astrea_step_timed", "astrea_reduce_conserved_static",
     "astrea_sweep_tile", "astrea_point_state", "astrea_total_variation", "astrea_solution_error",
-    "astrea_clock_async", "astrea_space_ct",
+    "astrea_clock_async", "astrea_space_ct", "astrea_step_host",
 ]
 
 
@@ -62,6 +62,7 @@ def load(path=LIB_PATH):
             "astrea_reset_clock": ([vp, d, i, i, vp], i),
             "astrea_step": ([vp, vp, i, vp], i),
             "astrea_graph_step": ([vp, vp, i, vp], i),
+            "astrea_step_host": ([vp, vp, vp, vp, vp], i),
             "astrea_get_clock": ([vp, dp, dp, ip, ip, ip, vp], i),
             "astrea_clock_async": ([vp, vp, vp, vp, vp], i),
             "astrea_space": ([vp, vp, i, vp, vp, dp, vp], i),

@@ -90,9 +90,19 @@ struct IEngine {
   double* sums = nullptr;
   cudaGraphExec_t graph = nullptr;
   void* graph_state = nullptr;
+  // astrea_step_host: a captured step with host input and output, and its buffers
+  cudaGraphExec_t graph_host = nullptr;
+  const void* graph_host_key[3] = {nullptr, nullptr, nullptr};
+  // device-accessible address of page-locked host memory for the final stage's combine to write
+  // the state into while it computes (nullptr: the result is copied after the step)
+  void* host_out = nullptr;
   cudaStream_t graph_stream = nullptr;
+  // whether enqueue_step stores the final state to host_out itself (the SSP-RK paths whose last
+  // stage ends in a combining sweep); otherwise the caller copies it after the step
+  virtual bool fuses_host_out() const = 0;
   virtual ~IEngine() {
     if (graph) cudaGraphExecDestroy(graph);
+    if (graph_host) cudaGraphExecDestroy(graph_host);
     cudaFree(clk);
     cudaFree(part);
     cudaFree(sums);
@@ -555,6 +565,10 @@ template <typename T> struct Engine final : IEngine {
     return ASTREA_OK;
   }
 
+  bool fuses_host_out() const override {
+    return !ct() && cfg.integrator < SSPRK53 && stages_of(cfg.integrator) >= 2;
+  }
+
   int enqueue_step(void* state, Clock* c, bool device_dt, cudaStream_t st, KTimer* tm = nullptr) override {
     T* u = static_cast<T*>(state);
     if (cfg.integrator >= SSPRK53) return enqueue_step_rk(u, c, device_dt, st, tm);
@@ -601,6 +615,7 @@ template <typename T> struct Engine final : IEngine {
       a.stage = s;
       a.u0 = u;
       a.out = out;
+      if (s == ns - 1) a.out_host = static_cast<T*>(host_out);
       int prc = prep(cur, c, st, tm);
       if (prc) return prc;
       if (cfg.dim == 2) {
@@ -885,6 +900,55 @@ int astrea_graph_step(astrea_handle* h, void* state, int nsteps, void* stream) {
     e->graph_state = state;
   }
   for (int i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(e->graph, st));
+  return ASTREA_OK;
+}
+
+int astrea_step_host(astrea_handle* h, void* state, const void* host_in, void* host_out, void* stream) {
+  if (!h || !state) return fail(ASTREA_ERR_ARG, "NULL argument");
+  IEngine* e = h->eng;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int trc = e->prepare(state, st);
+  if (trc) return trc;
+  const size_t bytes = (size_t)e->nv * (size_t)e->cells * (e->cfg.precision == 64 ? 8 : 4);
+  // host_out is written by the kernels only where it is page-locked memory the device can address
+  void* out_dev = nullptr;
+  if (host_out) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, host_out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+      out_dev = pa.devicePointer;
+    cudaGetLastError();  // a pageable pointer is not an error here
+  }
+  const bool fused = out_dev != nullptr && e->fuses_host_out();
+  if (!e->graph_host || e->graph_host_key[0] != state || e->graph_host_key[1] != host_in ||
+      e->graph_host_key[2] != host_out) {
+    if (e->graph_host) {
+      cudaGraphExecDestroy(e->graph_host);
+      e->graph_host = nullptr;
+    }
+    cudaStream_t cap;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed));
+    cudaError_t me = cudaSuccess;
+    if (host_in) me = cudaMemcpyAsync(state, host_in, bytes, cudaMemcpyHostToDevice, cap);
+    e->host_out = fused ? out_dev : nullptr;
+    int rc = me == cudaSuccess ? e->enqueue_step(state, e->clk, true, cap) : ASTREA_OK;
+    e->host_out = nullptr;
+    if (rc == ASTREA_OK && me == cudaSuccess && host_out && !fused)
+      me = cudaMemcpyAsync(host_out, state, bytes, cudaMemcpyDeviceToHost, cap);
+    cudaError_t ce = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc) return rc;
+    if (me != cudaSuccess) return cuda_fail(me, "cudaMemcpyAsync (host state)");
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+    ce = cudaGraphInstantiate(&e->graph_host, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+    e->graph_host_key[0] = state;
+    e->graph_host_key[1] = host_in;
+    e->graph_host_key[2] = host_out;
+  }
+  CK(cudaGraphLaunch(e->graph_host, st));
   return ASTREA_OK;
 }
 

@@ -66,6 +66,7 @@ template <typename T> struct SweepArgs {
   const T* dother;    // mode 1: divergence of the other sweep
   const T* u0;        // step-start state
   T* out;             // combine output
+  T* out_host;        // optional: the combine output also stored to page-locked host memory (same layout)
   Clock* clock;
   T* flux_out;        // optional: interface fluxes [NV][Ns+1][Nt]
   T* wface_out;       // optional (2D MHD): face value at i+1/2 of every cell, physical layout [8][n0][n1]
@@ -908,7 +909,9 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
           const T L = -total;
           const T u = a.u0[s * a.plane + g];
           const T cur = a.q[s * a.plane + g];
-          a.out[s * a.plane + g] = combine<T>(a.integ, a.stage, u, cur, L, dtT);
+          const T v = combine<T>(a.integ, a.stage, u, cur, L, dtT);
+          a.out[s * a.plane + g] = v;
+          if (a.out_host) a.out_host[s * a.plane + g] = v;  // the step's result straight to the host
         }
       }
     }

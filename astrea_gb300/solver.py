@@ -196,6 +196,14 @@ class Solver:
         fn = self.lib.astrea_graph_step if graph else self.lib.astrea_step
         _lib.check(fn(self.handle, ctypes.c_void_p(self.state.data_ptr()), int(n), _stream()))
 
+    def step_host(self, host_in, host_out):
+        """One step with the state taken from ``host_in`` and the result left in ``host_out`` (host
+        tensors in the state layout; page-locked ones let the last sweep write the result directly)."""
+        vp = ctypes.c_void_p
+        _lib.check(self.lib.astrea_step_host(self.handle, vp(self.state.data_ptr()),
+                                             vp(host_in.data_ptr() if host_in is not None else 0),
+                                             vp(host_out.data_ptr() if host_out is not None else 0), _stream()))
+
     def clock(self):
         t, dt = ctypes.c_double(), ctypes.c_double()
         steps, done, status = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

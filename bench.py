@@ -1001,24 +1001,38 @@ def main():
     del s64
     torch.cuda.empty_cache()
 
-    # ---- end to end through the C ABI with host buffers (pinned): H2D state, one step, D2H state
+    # ---- end to end through the C ABI with host buffers (pinned): every step copies the state in
+    # from page-locked host memory and leaves its result there (astrea_step_host: the last sweep of
+    # the step writes the result to the host buffer while it computes); the result of one step is
+    # the input of the next, as in a caller that keeps the grid on the host
     host = torch.empty_like(s32.state, device="cpu").pin_memory()
     host.copy_(s32.state.cpu())
     for _ in range(2):
-        s32.state.copy_(host, non_blocking=True)
-        s32.step(1, graph=True)
-        host.copy_(s32.state, non_blocking=True)
+        s32.step_host(host, host)
     torch.cuda.synchronize()
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     g0.record(stream)
     for _ in range(args.e2e_steps):
-        s32.state.copy_(host, non_blocking=True)
-        s32.step(1, graph=True)
-        host.copy_(s32.state, non_blocking=True)
+        s32.step_host(host, host)
     g1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = allmax(g0.elapsed_time(g1), ws)
     e2e = ws * cells * args.e2e_steps / (e2e_ms / 1e3)
+    # the same with the result copied out after the step (no fused host store), for comparison
+    h2 = host.clone().pin_memory()
+    for _ in range(2):
+        s32.state.copy_(h2, non_blocking=True)
+        s32.step(1, graph=True)
+        h2.copy_(s32.state, non_blocking=True)
+    torch.cuda.synchronize()
+    g0.record(stream)
+    for _ in range(args.e2e_steps):
+        s32.state.copy_(h2, non_blocking=True)
+        s32.step(1, graph=True)
+        h2.copy_(s32.state, non_blocking=True)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    e2e_copy = ws * cells * args.e2e_steps / (allmax(g0.elapsed_time(g1), ws) / 1e3)
     state_bytes = s32.state.numel() * s32.state.element_size()
     del s32
     torch.cuda.empty_cache()
@@ -1107,7 +1121,10 @@ def main():
             "gpu_launches": sum(launches),
             "launches_per_step": sum(launches) / args.steps,
             "e2e": {"value": e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
-                    "d2h_bytes_per_step": state_bytes, "steps": args.e2e_steps},
+                    "d2h_bytes_per_step": state_bytes, "steps": args.e2e_steps,
+                    "path": "astrea_step_host: H2D copy of the state, the step, the result stored to the pinned host "
+                            "buffer by the last sweep",
+                    "with_copy_after_step": e2e_copy},
             "batched": batched,
             "serving": serving,
             "mhd_orszag_tang": mhd,

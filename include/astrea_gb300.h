@@ -151,6 +151,20 @@ int astrea_sweep_tile(const astrea_handle* h, int axis, int* ts, int* tt);
  * astrea.py:44-84). */
 int astrea_clock_async(astrea_handle* h, double* t, int* steps, int* done, void* stream);
 
+/* One step of the core_run loop (astrea.py:66-85) for a caller that keeps the
+ * grid in host memory between steps: ``host_in`` (nv planes of n0*n1
+ * elements, may be NULL) is copied into the device ``state`` first, the step
+ * runs with the device dt, and the stepped state is written to ``host_out``
+ * (may be NULL; may equal host_in).  Where host_out is page-locked memory the
+ * device can address (cudaHostAlloc / torch pin_memory) and the integrator's
+ * last stage ends in a combining sweep (SSP-RK (2,2), (3,3), (4,3) without
+ * constrained transport), that sweep stores the result to host_out while it
+ * computes, so no separate device-to-host copy follows the step; otherwise
+ * the state is copied after the step.  The sequence is captured once per
+ * (state, host_in, host_out) and replayed; asynchronous on ``stream``.  No
+ * counterpart in the reference (its grid always lives in host memory). */
+int astrea_step_host(astrea_handle* h, void* state, const void* host_in, void* host_out, void* stream);
+
 /* Read the device clock (synchronises ``stream``).  status bit 0: a
  * non-finite wave speed or dt was seen. */
 int astrea_get_clock(astrea_handle* h, double* t, double* dt, int* steps, int* done, int* status, void* stream);

@@ -796,8 +796,8 @@ def run_alone(r, precision, max_steps=200000):
 def serving_full(count, rates, seed=SEED, max_wall_s=1800.0, alone_sample=40, fp64_max_cells=512 * 512):
     """The serving workload at its configured size range (1D N log-U[256, 65536], 2D side log-U[128, 2048],
     150 GB budget): per arrival rate p50/p99 latency and cell-updates/s of the requests that finished cleanly;
-    every request that ended non-finite is solved again alone in FP64 (those of at most ``fp64_max_cells``
-    cells) to see whether the method or FP32 fails it; and a sample of requests solved one at a time by the
+    every request that ended non-finite is solved again alone in FP64 (2D ones of at most ``fp64_max_cells``
+    cells, 1D ones of at most 16384) to see whether the method or FP32 fails it; and a sample of requests solved one at a time by the
     single-grid solver, for the rate of the same work without batching."""
     import torch
     from astrea_gb300.serving import Server, make_requests
@@ -815,7 +815,7 @@ def serving_full(count, rates, seed=SEED, max_wall_s=1800.0, alone_sample=40, fp
         failed = [r for r in reqs if r.status & 1]
         rerun = []
         for r in failed:
-            if r.cells <= fp64_max_cells:
+            if (r.dim == 2 and r.cells <= fp64_max_cells) or (r.dim == 1 and r.n <= 16384):
                 st, steps, _ = run_alone(r, 64)
                 rerun.append({"rid": r.rid, "dim": r.dim, "n": r.n, "mhd": r.mhd, "scheme": r.scheme,
                               "solver": r.solver, "status32": r.status, "status64": st, "steps64": steps})

@@ -168,18 +168,29 @@ template <typename T, int AX, int TS, int TT> struct StripBox {
   }
 };
 
-// WSIN: the tile stages the precomputed wS level and has no q level.
+// Cell-interleaved levels (the face values R, the five face arrays and the final fluxes F)
+// hold the variables of one cell side by side, padded to a whole number of 16-byte units, so
+// that a cell's variables move with one or two vector loads and stores: the element (li, s)
+// of such a level is at li * NVP + s.  The staged levels (q, its primitives, wS) keep one plane
+// per variable, which the along-the-sweep stencils read one variable at a time.
+template <int NV> struct Interleave {
+  static constexpr int NVP = NV == 3 ? 4 : NV;
+};
+
+// WSIN: the tile stages the precomputed wS level and has no q level.  Every level starts at a
+// multiple of four elements (16 bytes or more) from the 16-byte aligned dynamic shared memory.
 template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Smem {
   using G = Geom<SCH, DIM, TS, TT>;
-  static constexpr int n_q = WSIN ? 0 : NV * G::QH * G::QW;
+  static constexpr int NVP = Interleave<NV>::NVP;
+  static constexpr int n_q = WSIN ? 0 : ceil_to(NV * G::QH * G::QW, 4);
   static constexpr int n_qw = G::HO ? n_q : 0;
-  static constexpr int n_face = DIM == 2 ? 5 * NV * G::FH * G::KW : 0;
-  static constexpr int n_F = NV * TT * G::KW;
+  static constexpr int n_face = DIM == 2 ? 5 * NVP * G::FH * G::KW : 0;
+  static constexpr int n_F = NVP * TT * G::KW;
   // the face arrays reuse the q level once it is dead; PCM reads raw q on faces, so it keeps q
   static constexpr int FA_OFF = SCH == PCM ? n_q : 0;
-  static constexpr int n_region0 = (n_q + n_qw) > (FA_OFF + n_face + n_F) ? (n_q + n_qw) : (FA_OFF + n_face + n_F);
-  static constexpr int n_w = NV * G::WH * G::WW;
-  static constexpr int n_R = 2 * NV * G::RH * G::RW;
+  static constexpr int n_region0 = ceil_to((n_q + n_qw) > (FA_OFF + n_face + n_F) ? (n_q + n_qw) : (FA_OFF + n_face + n_F), 4);
+  static constexpr int n_w = ceil_to(NV * G::WH * G::WW, 4);
+  static constexpr int n_R = 2 * NVP * G::RH * G::RW;
   static constexpr int n_lam = G::FH * G::YW;
   static constexpr int base = n_region0 + n_w + n_R + n_lam + 64;
   // PPM extras: flattening coefficients on the rows of the face level and the
@@ -190,7 +201,7 @@ template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Sm
   // The coefficients need chi_bar one column further on each side (n_cb).
   static constexpr int n_eta = SCH == PPM ? G::RH * (G::RW + 1) : 0;
   static constexpr int n_cb = SCH == PPM ? G::RH * (G::RW + 3) : 0;
-  static constexpr int n_mu = SCH == PPM ? NV * TT * G::KW : 0;
+  static constexpr int n_mu = SCH == PPM ? NVP * TT * G::KW : 0;  // interleaved like F (it sits where F goes)
   static constexpr bool MU_IN_F = DIM == 2;
   static constexpr bool ETA_IN_GAP = DIM == 2 && (n_q + n_qw + n_eta + n_cb <= FA_OFF + n_face);
   static constexpr int MU_OFF = MU_IN_F ? FA_OFF + n_face : base;
@@ -217,6 +228,41 @@ template <class M, typename T> __device__ __forceinline__ void load_sm(const T* 
 template <class M, typename T> __device__ __forceinline__ void store_sm(T* base, int stride, int idx, const T* x) {
 #pragma unroll
   for (int s = 0; s < M::NV; ++s) base[s * stride + idx] = x[M::var(s)];
+}
+
+// Element li of a cell-interleaved level (16-byte vector accesses: the level's base and
+// li * NVP * sizeof(T) are multiples of 16 bytes by construction of Smem)
+template <class M, typename T> __device__ __forceinline__ void load_aos(const T* base, int li, T* x) {
+  constexpr int NVP = Interleave<M::NV>::NVP, PER = 16 / (int)sizeof(T);
+  static_assert(NVP % PER == 0, "a cell's interleaved variables fill whole 16-byte units");
+  T v[NVP];
+  const T* p = base + li * NVP;
+#pragma unroll
+  for (int c = 0; c < NVP / PER; ++c) {
+    if constexpr (sizeof(T) == 4) {
+      const float4 u = reinterpret_cast<const float4*>(p)[c];
+      v[4 * c] = u.x; v[4 * c + 1] = u.y; v[4 * c + 2] = u.z; v[4 * c + 3] = u.w;
+    } else {
+      const double2 u = reinterpret_cast<const double2*>(p)[c];
+      v[2 * c] = u.x; v[2 * c + 1] = u.y;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = T(0);
+#pragma unroll
+  for (int s = 0; s < M::NV; ++s) x[M::var(s)] = v[s];
+}
+template <class M, typename T> __device__ __forceinline__ void store_aos(T* base, int li, const T* x) {
+  constexpr int NVP = Interleave<M::NV>::NVP, PER = 16 / (int)sizeof(T);
+  T v[NVP];
+#pragma unroll
+  for (int s = 0; s < NVP; ++s) v[s] = s < M::NV ? x[M::var(s < M::NV ? s : 0)] : T(0);
+  T* p = base + li * NVP;
+#pragma unroll
+  for (int c = 0; c < NVP / PER; ++c) {
+    if constexpr (sizeof(T) == 4) reinterpret_cast<float4*>(p)[c] = make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+    else reinterpret_cast<double2*>(p)[c] = make_double2(v[2 * c], v[2 * c + 1]);
+  }
 }
 
 // Stage combines (evolvers.py:150-185), with the reference's operation order
@@ -273,6 +319,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   using S = Smem<SCH, DIM, TS, TT, M::NV, WSIN>;
   static_assert(!WSIN || (DIM == 2 && G::HO), "precomputed wS is for 2D high-order tiles");
   static_assert(!TMA || WSIN || !G::HO, "the TMA box holds the wS level: high-order tiles stage it precomputed");
+  static_assert(S::FA_OFF % 4 == 0 && S::n_face % 4 == 0 && S::n_region0 % 4 == 0 && S::n_w % 4 == 0 &&
+                    S::n_R % 4 == 0 && S::n_F % 4 == 0,
+                "cell-interleaved levels start on 16-byte boundaries");
+  constexpr int NVP = Interleave<M::NV>::NVP;
   constexpr int NV = M::NV;
   T* sm = reinterpret_cast<T*>(smem_raw);
   T* s_q = sm;                       // region 0 (a): q and its point primitives
@@ -607,14 +657,14 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
               using SB = StripBox<T, AX, TS, TT>;
 #pragma unroll
               for (int v = 0; v < NV; ++v)
-                s_mu[(v * TT + row) * W + col] =
+                s_mu[(row * W + col) * NVP + v] =
                     a.av_alpha * (nu * (qs_box[SB::at(v, xp, rt, s0, t0)] - qs_box[SB::at(v, x, rt, s0, t0)]));
             } else {
               const T* qrow = sm + S::QS_OFF + (rt - t0) * S::QSW - (s0 - 1);
 #pragma unroll
               for (int v = 0; v < NV; ++v) {
                 const T* qv = qrow + v * TT * S::QSW;
-                s_mu[(v * TT + row) * W + col] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+                s_mu[(row * W + col) * NVP + v] = a.av_alpha * (nu * (qv[xp] - qv[x]));
               }
             }
           } else {
@@ -622,7 +672,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
               const T* qv = qrow + v * G::QH * G::QW;
-              s_mu[(v * TT + row) * W + col] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+              s_mu[(row * W + col) * NVP + v] = a.av_alpha * (nu * (qv[xp] - qv[x]));
             }
           }
         }
@@ -642,12 +692,12 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       const int s = rem / H, row = rem % H, col0 = strip * K;
       const int vs0 = s0 + G::R_BEG + col0, vt = t0 - G::RT + row;
       const T* wrow = s_w + (s * WH + row + (G::WT - G::RT)) * WW - (s0 + G::W_BEG);
-      T* rl = s_R + ((0 * NV + s) * H + row) * W + col0;
-      T* rr = s_R + ((1 * NV + s) * H + row) * W + col0;
+      T* rl = s_R + (row * W + col0) * NVP + s;
+      T* rr = rl + NVP * H * W;
       const T* erow = a.flatten ? s_eta + row * (W + 1) - (s0 + G::R_BEG - 1) : nullptr;
       recon_ppm_strip<T, K>([&](int x) -> T { return wrow[x]; }, vs0, [&](int k, T wl, T wr, T fr) {
-        rl[k] = wl;
-        rr[k] = wr;
+        rl[k * NVP] = wl;
+        rr[k * NVP] = wr;
         const int vs = vs0 + k;
         if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt)
           a.wface_out[M::var(s) * a.plane + gidx(vs, vt)] = fr;
@@ -665,8 +715,8 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       const T* erow = (SCH == PPM && a.flatten) ? s_eta + row * (W + 1) - (s0 + G::R_BEG - 1) : nullptr;
       T wl, wr;
       reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr, erow);
-      s_R[((0 * NV + s) * H + row) * W + col] = wl;
-      s_R[((1 * NV + s) * H + row) * W + col] = wr;
+      s_R[(row * W + col) * NVP + s] = wl;
+      s_R[NVP * H * W + (row * W + col) * NVP + s] = wr;
       if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) {
         // the face value the constrained transport uses: PPM's unlimited 4th-order
         // face (ppm.py:38-42), the right face value of the other schemes (weno.py:168, plm.py:39)
@@ -682,10 +732,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 
   // accessors into the R level: virtual cell x (already mapped), real row rt
   auto loadL = [&](int x, int rt, T* out) {
-    load_sm<M>(s_R, G::RH * G::RW, (rt - (t0 - G::RT)) * G::RW + (x - (s0 + G::R_BEG)), out);
+    load_aos<M>(s_R, (rt - (t0 - G::RT)) * G::RW + (x - (s0 + G::R_BEG)), out);
   };
   auto loadR = [&](int x, int rt, T* out) {
-    load_sm<M>(s_R + NV * G::RH * G::RW, G::RH * G::RW, (rt - (t0 - G::RT)) * G::RW + (x - (s0 + G::R_BEG)), out);
+    load_aos<M>(s_R + NVP * G::RH * G::RW, (rt - (t0 - G::RT)) * G::RW + (x - (s0 + G::R_BEG)), out);
   };
 
   // ---- level lambda: wave speed of the interface average right of each cell (fv.compute_eigen)
@@ -794,19 +844,19 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       if constexpr (SCH == PPM) {
         if (a.viscosity) {
 #pragma unroll
-          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + s_mu[v * TT * W + e];
+          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + s_mu[e * NVP + v];
         }
       }
-      store_sm<M>(s_F, TT * W, e, F);
+      store_aos<M>(s_F, e, F);
     }
   } else {
     // ---- 2D level A: face-averaged solve on rows t0-1 .. t0+TT
     constexpr int W = G::KW, H = G::FH;
     T* s_qp = s_fa;
-    T* s_qm = s_fa + NV * H * W;
-    T* s_fp = s_fa + 2 * NV * H * W;
-    T* s_fm = s_fa + 3 * NV * H * W;
-    T* s_Fa = s_fa + 4 * NV * H * W;
+    T* s_qm = s_fa + NVP * H * W;
+    T* s_fp = s_fa + 2 * NVP * H * W;
+    T* s_fm = s_fa + 3 * NVP * H * W;
+    T* s_Fa = s_fa + 4 * NVP * H * W;
     // items with the R level's row pitch (conflict-free loads across a row change)
     for (int e = tid; e < G::RW * H; e += nth) {
       const int row = e / G::RW, col = e % G::RW;
@@ -823,11 +873,11 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       if constexpr (SOL == HLLD) load_wS(rs_(vk), rt, wSr);
       solve(col, row, wSr, wp, wm, qp, qm, fp, fm, F);
       const int li = row * W + col;
-      store_sm<M>(s_qp, H * W, li, qp);
-      store_sm<M>(s_qm, H * W, li, qm);
-      store_sm<M>(s_fp, H * W, li, fp);
-      store_sm<M>(s_fm, H * W, li, fm);
-      store_sm<M>(s_Fa, H * W, li, F);
+      store_aos<M>(s_qp, li, qp);
+      store_aos<M>(s_qm, li, qm);
+      store_aos<M>(s_fp, li, fp);
+      store_aos<M>(s_fm, li, fm);
+      store_aos<M>(s_Fa, li, F);
     }
     __syncthreads();
     // ---- 2D level B: face-centred states (fv.high_order_convert 'avg'/'face'), second solve, F_c - d2 F_avg
@@ -847,17 +897,17 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       conv(cwp);
       loadR(rs_(vk - 1), rt, x0); loadR(rs_(vk - 1), rm, xm); loadR(rs_(vk - 1), rp, xp);
       conv(cwm);
-      load_sm<M>(s_qp, H * W, fr * W + col, x0); load_sm<M>(s_qp, H * W, frm * W + col, xm); load_sm<M>(s_qp, H * W, frp * W + col, xp);
+      load_aos<M>(s_qp, fr * W + col, x0); load_aos<M>(s_qp, frm * W + col, xm); load_aos<M>(s_qp, frp * W + col, xp);
       conv(cqp);
-      load_sm<M>(s_qm, H * W, fr * W + col, x0); load_sm<M>(s_qm, H * W, frm * W + col, xm); load_sm<M>(s_qm, H * W, frp * W + col, xp);
+      load_aos<M>(s_qm, fr * W + col, x0); load_aos<M>(s_qm, frm * W + col, xm); load_aos<M>(s_qm, frp * W + col, xp);
       conv(cqm);
-      load_sm<M>(s_fp, H * W, fr * W + col, x0); load_sm<M>(s_fp, H * W, frm * W + col, xm); load_sm<M>(s_fp, H * W, frp * W + col, xp);
+      load_aos<M>(s_fp, fr * W + col, x0); load_aos<M>(s_fp, frm * W + col, xm); load_aos<M>(s_fp, frp * W + col, xp);
       conv(cfp);
-      load_sm<M>(s_fm, H * W, fr * W + col, x0); load_sm<M>(s_fm, H * W, frm * W + col, xm); load_sm<M>(s_fm, H * W, frp * W + col, xp);
+      load_aos<M>(s_fm, fr * W + col, x0); load_aos<M>(s_fm, frm * W + col, xm); load_aos<M>(s_fm, frp * W + col, xp);
       conv(cfm);
       if constexpr (SOL == HLLD) load_wS(rs_(vk), rt, wSr);
       solve(col, fr, wSr, cwp, cwm, cqp, cqm, cfp, cfm, Fc);
-      load_sm<M>(s_Fa, H * W, fr * W + col, x0); load_sm<M>(s_Fa, H * W, frm * W + col, xm); load_sm<M>(s_Fa, H * W, frp * W + col, xp);
+      load_aos<M>(s_Fa, fr * W + col, x0); load_aos<M>(s_Fa, frm * W + col, xm); load_aos<M>(s_Fa, frp * W + col, xp);
       T F[8];
 #pragma unroll
       for (int i = 0; i < 8; ++i) F[i] = sub_d2_24<T>(Fc[i], x0[i], xm[i], xp[i]);
@@ -865,10 +915,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         // the viscous flux of this interface sits where F goes: read it, then overwrite
         if (a.viscosity) {
 #pragma unroll
-          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + s_mu[(v * TT + row) * W + col];
+          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + s_mu[(row * W + col) * NVP + v];
         }
       }
-      store_sm<M>(s_F, TT * W, row * W + col, F);
+      store_aos<M>(s_F, row * W + col, F);
     }
   }
   __syncthreads();
@@ -884,7 +934,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       const long long fidx = (long long)vk * Nt + vt;
       const long long fplane = (long long)(Ns + 1) * Nt;
 #pragma unroll
-      for (int s = 0; s < NV; ++s) a.flux_out[s * fplane + fidx] = s_F[(s * TT + row) * W + col];
+      for (int s = 0; s < NV; ++s) a.flux_out[s * fplane + fidx] = s_F[(row * W + col) * NVP + s];
     }
   }
 
@@ -899,9 +949,12 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       const int vs = s0 + col, vt = t0 + row;
       if (vs >= Ns || vt >= Nt) continue;
       const long long g = gidx(vs, vt);
+      T Fr[8], Fl[8];
+      load_aos<M>(s_F, row * W + col + 1, Fr);
+      load_aos<M>(s_F, row * W + col, Fl);
 #pragma unroll
       for (int s = 0; s < NV; ++s) {
-        const T D = (s_F[(s * TT + row) * W + col + 1] - s_F[(s * TT + row) * W + col]) / dxT;
+        const T D = (Fr[M::var(s)] - Fl[M::var(s)]) / dxT;
         if (a.mode == 0) {
           a.dout[s * a.plane + g] = D;
         } else {

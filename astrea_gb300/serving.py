@@ -50,7 +50,7 @@ class Request:
     seed: int
     boundary: str = "edge"
     gamma: float = 1.4
-    cfl: float = 0.8
+    cfl: float = 0.8  # make_requests: 0.8 in 1D, 0.4 in 2D
     compat: bool = False
     # filled in by the server
     admitted: float = math.nan
@@ -130,8 +130,11 @@ def make_requests(count, rate, seed=20261203, n1d=(256, 65536), n2d=(128, 2048),
         mhd = bool(rng.uniform() < frac_mhd)
         scheme = ["plm", "ppm", "weno5"][rng.integers(3)]
         solver = ["llf", "hlld" if mhd else "hllc"][rng.integers(2)]
+        # the reference's dt rule takes the CFL number per axis (astrea.py:70-71), which the
+        # unsplit 2D update adds over both axes: 0.4 keeps that sum at 0.8, as 0.8 does in 1D
         out.append(Request(rid=i, arrival=t, dim=dim, n=n, mhd=mhd, scheme=scheme, solver=solver,
-                           t_end=float(rng.uniform(*t_end)), seed=int(rng.integers(1 << 31))))
+                           t_end=float(rng.uniform(*t_end)), seed=int(rng.integers(1 << 31)),
+                           cfl=0.8 if dim == 1 else 0.4))
     return out
 
 

@@ -767,7 +767,7 @@ def serving_leg(count, rates, seed=SEED, max_wall_s=30.0):
     head = dict(sweep[0])
     head.update({"rates": sweep, "requests_per_rate": count,
                  "mix": "40% 1D N log-U[64,16384], 60% 2D side log-U[32,512] (the full mix / 4 per axis), "
-                        "Euler|MHD 50/50, {PLM,PPM,WENO5}x{LLF,HLLC|HLLD}, t_end U[.05,.3], FP32",
+                        "Euler|MHD 50/50, {PLM,PPM,WENO5}x{LLF,HLLC|HLLD}, t_end U[.05,.3], CFL 0.8 (1D) / 0.4 (2D), FP32",
                  "hbm_budget_gb": 150})
     return head
 
@@ -803,7 +803,7 @@ def serving_full(count, rates, seed=SEED, max_wall_s=1800.0, alone_sample=40, fp
     from astrea_gb300.serving import Server, make_requests
     srv = Server(hbm_budget_bytes=150e9, precision=32, max_slots=256, steps_per_poll=8, max_steps=200000)
     out = {"mix": "40% 1D N log-U[256,65536], 60% 2D side log-U[128,2048], Euler|MHD 50/50, "
-                  "{PLM,PPM,WENO5}x{LLF,HLLC|HLLD}, t_end U[.05,.3], FP32, HBM budget 150 GB",
+                  "{PLM,PPM,WENO5}x{LLF,HLLC|HLLD}, t_end U[.05,.3], CFL 0.8 (1D) / 0.4 (2D), FP32, HBM budget 150 GB",
            "requests_per_rate": count, "rates": []}
     for i, rate in enumerate(rates):
         reqs = make_requests(count, rate, seed=seed + i)

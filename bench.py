@@ -1110,6 +1110,10 @@ def main():
             "fp64_plain": {"value": value64, "unit": "cell-updates/s", "steps": args.fp64_steps,
                            "ms_per_step": ms64 / args.fp64_steps},
             "fp32_over_fp64": value / ws / value64,
+            # same precision against the reference's algorithm on the host: the FP64 plain GPU path over
+            # the oracle on one core (FP64, LAPACK wave speeds); the reference arm runs it on every core
+            "fp64_over_cpu_baseline_per_core": (value64 / cpu["value"]) if isinstance(cpu, dict) and cpu.get("value")
+                                               else None,
             "l1_rho_fp32_vs_fp64": (accuracy.get("series") or [{}])[0].get("l1_rho_fp32_vs_fp64")
                                    if isinstance(accuracy, dict) else None,
             "l1_at_t": 0.05,

@@ -257,18 +257,31 @@ def test_textbook_hlld_orszag_tang_matches_oracle(scheme):
 
 
 def test_fp32_against_fp64_shear_layer():
-    # FP32 bulk arithmetic (FP64 pressure recovery): L1(rho) against the FP64 run after 10 steps.
-    # Measured 1.27e-5 on GB300 at 64^2 (limiter branches that flip between precisions
-    # dominate); the bar below is 2e-5.  The full-size figure is reported by bench.py.
+    """FP32 bulk arithmetic (FP64 pressure recovery) against FP64 on the shear layer, 10 steps at 64^2.
+
+    The error measure is L1(rho).  The flow amplifies any perturbation (limiter branches flip at
+    the sharp shear interfaces), so the bar is relative to what round-off does to FP64 itself: an
+    FP64 twin started with every cell's density one ulp up or down.  FP32 must stay within the
+    1e-5 target or within four times the twin's distance, whichever is larger (bench.py and
+    profiles/ report the same comparison at full size and up to t=1.0).
+    """
     n = 64
     w = shear_layer(n)
-    a, b = Solver(shear_cfg(n, 64)), Solver(shear_cfg(n, 32))
-    for s in (a, b):
+    a, b, c = Solver(shear_cfg(n, 64)), Solver(shear_cfg(n, 32)), Solver(shear_cfg(n, 64))
+    for s in (a, b, c):
         s.initialise(w)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    up = (torch.rand(c.state[0].shape, generator=g) < .5).to(c.state.device)
+    rho = c.state[0].clone()
+    c.state[0] = torch.where(up, torch.nextafter(rho, torch.full_like(rho, float("inf"))),
+                             torch.nextafter(rho, torch.full_like(rho, -float("inf"))))
+    for s in (a, b, c):
         s.reset_clock()
         s.step(10)
     l1 = float(torch.mean(torch.abs(b.state[0].double() - a.state[0])).item())
-    assert l1 <= 2e-5, l1
+    l1_twin = float(torch.mean(torch.abs(c.state[0] - a.state[0])).item())
+    assert 0 < l1_twin
+    assert l1 <= max(1e-5, 4 * l1_twin), (l1, l1_twin)
     assert abs(a.clock()["t"] - b.clock()["t"]) <= 1e-5 * a.clock()["t"]
 
 

@@ -69,16 +69,12 @@ __device__ __forceinline__ void ppm_mc_limit(T w0, T wm1, T wp1, T wm2, T wp2, T
   const T curv = npsign(d2c) * npmin(npmin(abs_(d2w), C * abs_(d2c)), npmin(C * abs_(d2c_p), C * abs_(d2c_m)));
   const T d2w_lim = extremum ? curv : T(0);
   const T scale = npmax(abs_(w0), npmax(npmax(abs_(wm1), abs_(wp1)), npmax(abs_(wm2), abs_(wp2))));
-  // the curvature is trusted only above round-off: 1e-12 of the stencil's magnitude in FP64 (the
-  // reference's threshold), 1e-5 in FP32, where six times a sum of four values already carries
-  // ~1e-6 of it in rounding (a smaller FP32 threshold lets noise decide the limiter's branch)
-  constexpr double kSens = Prec<T>::EXACT ? 1e-12 : 1e-5, kOne = Prec<T>::EXACT ? 1.0 - 1e-12 : 1.0 - 1e-6;
-  const bool sensitive = abs_(d2w) > T(kSens) * scale;
+  const bool sensitive = abs_(d2w) > T(1e-12) * scale;
   const T phi = dvd(d2w_lim, d2w);
   const T rl = sensitive ? phi : T(0);
   const T d3min = npmin(npmin(d3_m1, d3), npmin(d3_m2, d3_p2));
   const T d3max = npmax(npmax(d3_m1, d3), npmax(d3_m2, d3_p2));
-  const bool limit = (rl < T(kOne)) || (T(.1) * npmax(abs_(d3max), abs_(d3min)) <= (d3max - d3min));
+  const bool limit = (rl < T(1.0 - 1e-12)) || (T(.1) * npmax(abs_(d3max), abs_(d3min)) <= (d3max - d3min));
   T L = fL, R = fR;
   if ((dwm * dwp < T(0)) && limit) {
     L = w0 - rl * dwm;

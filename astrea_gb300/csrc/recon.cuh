@@ -66,12 +66,19 @@ __device__ __forceinline__ void ppm_mc_limit(T w0, T wm1, T wp1, T wm2, T wp2, T
   const T dwm = w0 - fL, dwp = fR - w0;
   const T d2w = T(6) * ((fL - T(2) * w0) + fR);
   const bool extremum = (dwm * dwp <= T(0)) || ((w0 - wm2) * (wp2 - w0) <= T(0));
-  const T curv = npsign(d2c) * npmin(npmin(abs_(d2w), C * abs_(d2c)), npmin(C * abs_(d2c_p), C * abs_(d2c_m)));
-  const T d2w_lim = extremum ? curv : T(0);
+  const T cmin = npmin(npmin(abs_(d2w), C * abs_(d2c)), npmin(C * abs_(d2c_p), C * abs_(d2c_m)));
   const T scale = npmax(abs_(w0), npmax(npmax(abs_(wm1), abs_(wp1)), npmax(abs_(wm2), abs_(wp2))));
   const bool sensitive = abs_(d2w) > T(1e-12) * scale;
-  const T phi = dvd(d2w_lim, d2w);
-  const T rl = sensitive ? phi : T(0);
+  T rl;
+  if constexpr (Prec<T>::EXACT) {
+    const T d2w_lim = extremum ? npsign(d2c) * cmin : T(0);
+    rl = sensitive ? dvd(d2w_lim, d2w) : T(0);
+  } else {
+    // FP32: sign(d2c) * cmin is cmin with d2c's sign (cmin is 0 where d2c is), and a
+    // sensitive d2w is non-zero, so the quotient needs no zero test
+    const T d2w_lim = extremum ? copysignf(cmin, d2c) : T(0);
+    rl = sensitive ? __fdividef(d2w_lim, d2w) : T(0);
+  }
   const T d3min = npmin(npmin(d3_m1, d3), npmin(d3_m2, d3_p2));
   const T d3max = npmax(npmax(d3_m1, d3), npmax(d3_m2, d3_p2));
   const bool limit = (rl < T(1.0 - 1e-12)) || (T(.1) * npmax(abs_(d3max), abs_(d3min)) <= (d3max - d3min));

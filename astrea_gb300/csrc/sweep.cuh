@@ -457,7 +457,9 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       }
       __syncthreads();  // the barrier is initialised before anyone waits on it
       if (!strip_tma) stage_strip();
-      const bool landed = mbar_wait_timed(&s_bar, 0, kCopyWaitNs);
+      // one warp polls the barrier; the others sleep in the block barrier, which then
+      // orders the copied data (visible to the polling warp) before their reads
+      const bool landed = tid < 32 ? mbar_wait_timed(&s_bar, 0, kCopyWaitNs) : true;
       if (!__syncthreads_and(landed)) {
         // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
         if (tid == 0) {
@@ -500,7 +502,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       else tma_load_3d(stage, map, B::x0(s0, t0), s0 + G::Q_BEG, 0, &s_bar);
     }
     __syncthreads();  // the barrier is initialised before anyone waits on it
-    const bool landed = mbar_wait_timed(&s_bar, 0, kCopyWaitNs);
+    const bool landed = tid < 32 ? mbar_wait_timed(&s_bar, 0, kCopyWaitNs) : true;  // one warp polls
     if (!__syncthreads_and(landed)) {
       // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
       if (tid == 0) {

@@ -39,6 +39,18 @@ template <typename T> __device__ __forceinline__ T npsign(T a) { return a > T(0)
 // fv.divide: a/b where b != 0 else 0
 template <typename T> __device__ __forceinline__ T dvd(T a, T b) { return b != T(0) ? a / b : T(0); }
 template <typename T> __device__ __forceinline__ T sq(T a) { return a * a; }
+// FP32 three-input minimum / maximum (one instruction on sm_100 and later); a NaN operand is
+// dropped, as in fminf / fmaxf
+__device__ __forceinline__ float fmin3_(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float fmax3_(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
 template <typename T> __device__ __forceinline__ T sqrt_(T a) { return sqrt(a); }
 template <> __device__ __forceinline__ float sqrt_<float>(float a) { return sqrtf(a); }
 template <typename T> __device__ __forceinline__ T abs_(T a) { return fabs(a); }

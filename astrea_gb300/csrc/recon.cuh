@@ -66,21 +66,28 @@ __device__ __forceinline__ void ppm_mc_limit(T w0, T wm1, T wp1, T wm2, T wp2, T
   const T dwm = w0 - fL, dwp = fR - w0;
   const T d2w = T(6) * ((fL - T(2) * w0) + fR);
   const bool extremum = (dwm * dwp <= T(0)) || ((w0 - wm2) * (wp2 - w0) <= T(0));
-  const T cmin = npmin(npmin(abs_(d2w), C * abs_(d2c)), npmin(C * abs_(d2c_p), C * abs_(d2c_m)));
-  const T scale = npmax(abs_(w0), npmax(npmax(abs_(wm1), abs_(wp1)), npmax(abs_(wm2), abs_(wp2))));
-  const bool sensitive = abs_(d2w) > T(1e-12) * scale;
-  T rl;
+  // min(|d2w|, C|d2c|, C|d2c_p|, C|d2c_m|): C > 0 and rounding is monotone, so the three
+  // products' minimum is the product of the minimum (the same value, NaN included)
+  T rl, d3min, d3max;
   if constexpr (Prec<T>::EXACT) {
+    const T cmin = npmin(abs_(d2w), C * npmin(npmin(abs_(d2c), abs_(d2c_p)), abs_(d2c_m)));
+    const T scale = npmax(abs_(w0), npmax(npmax(abs_(wm1), abs_(wp1)), npmax(abs_(wm2), abs_(wp2))));
+    const bool sensitive = abs_(d2w) > T(1e-12) * scale;
     const T d2w_lim = extremum ? npsign(d2c) * cmin : T(0);
     rl = sensitive ? dvd(d2w_lim, d2w) : T(0);
+    d3min = npmin(npmin(d3_m1, d3), npmin(d3_m2, d3_p2));
+    d3max = npmax(npmax(d3_m1, d3), npmax(d3_m2, d3_p2));
   } else {
-    // FP32: sign(d2c) * cmin is cmin with d2c's sign (cmin is 0 where d2c is), and a
-    // sensitive d2w is non-zero, so the quotient needs no zero test
+    // FP32: three-input minima and maxima; sign(d2c) * cmin is cmin with d2c's sign (cmin
+    // is 0 where d2c is), and a sensitive d2w is non-zero, so the quotient needs no zero test
+    const T cmin = fminf(abs_(d2w), C * fmin3_(abs_(d2c), abs_(d2c_p), abs_(d2c_m)));
+    const T scale = fmax3_(fmax3_(abs_(w0), abs_(wm1), abs_(wp1)), abs_(wm2), abs_(wp2));
+    const bool sensitive = abs_(d2w) > T(1e-12) * scale;
     const T d2w_lim = extremum ? copysignf(cmin, d2c) : T(0);
     rl = sensitive ? __fdividef(d2w_lim, d2w) : T(0);
+    d3min = fmin3_(fminf(d3_m1, d3), d3_m2, d3_p2);
+    d3max = fmax3_(fmaxf(d3_m1, d3), d3_m2, d3_p2);
   }
-  const T d3min = npmin(npmin(d3_m1, d3), npmin(d3_m2, d3_p2));
-  const T d3max = npmax(npmax(d3_m1, d3), npmax(d3_m2, d3_p2));
   const bool limit = (rl < T(1.0 - 1e-12)) || (T(.1) * npmax(abs_(d3max), abs_(d3min)) <= (d3max - d3min));
   T L = fL, R = fR;
   if ((dwm * dwp < T(0)) && limit) {
@@ -93,14 +100,13 @@ __device__ __forceinline__ void ppm_mc_limit(T w0, T wm1, T wp1, T wm2, T wp2, T
   wR = R;
 }
 
-// PPM faces with the McCorquodale & Colella extremum-preserving limiter
-// (ppm.py:30-72 with author 'mc'; limiters.extrapolant_limiter, limiters.py:82-143).
-// For finite data the limiter's no-extremum-anywhere branch
-// (limiters.py:141-143) gives the same values as the main branch, so the main
-// branch is evaluated for every cell.
 // A face value at x+1/2 blended towards the cell value at x by the flattening
-// coefficient eta(x) (ppm.py:67 with apply_flattener): f * eta + w * (1 - eta).
-template <typename T> __device__ __forceinline__ T ppm_flatten(T f, T w, T eta) { return f * eta + w * (T(1) - eta); }
+// coefficient eta(x) (ppm.py:67 with apply_flattener): f * eta + w * (1 - eta);
+// FP32 as w + eta * (f - w) (one rounding less).
+template <typename T> __device__ __forceinline__ T ppm_flatten(T f, T w, T eta) {
+  if constexpr (Prec<T>::EXACT) return f * eta + w * (T(1) - eta);
+  else return w + eta * (f - w);
+}
 
 // ``eta`` (nullptr: no flattening) gives the flattening coefficient at a mapped cell index.
 template <typename T, class A, class RH>

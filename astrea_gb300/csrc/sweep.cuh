@@ -226,7 +226,7 @@ template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Sm
   static constexpr int n_w = ceil_to(NV * G::WH * G::WW, 4);
   static constexpr int n_R = 2 * NVP * G::RH * G::RW;
   static constexpr int n_lam = G::FH * G::YW;
-  static constexpr int base = n_region0 + n_w + n_R + n_lam + 64;
+  static constexpr int base = ceil_to(n_region0 + n_w + n_R + n_lam + 64, 4);
   // PPM extras: flattening coefficients on the rows of the face level and the
   // columns [s0-2, s0+TS+2), and the viscous face fluxes of the tile's interfaces.
   // In 2D the viscous fluxes sit where the final fluxes go (they are added there),
@@ -354,7 +354,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   static_assert(!WSIN || (DIM == 2 && G::HO), "precomputed wS is for 2D high-order tiles");
   static_assert(!TMA || WSIN || !G::HO, "the TMA box holds the wS level: high-order tiles stage it precomputed");
   static_assert(S::FA_OFF % 4 == 0 && S::n_face % 4 == 0 && S::n_region0 % 4 == 0 && S::n_w % 4 == 0 &&
-                    S::n_R % 4 == 0 && S::n_F % 4 == 0,
+                    S::n_R % 4 == 0 && S::n_F % 4 == 0 && (SCH != PPM || S::MU_OFF % 4 == 0),
                 "cell-interleaved levels start on 16-byte boundaries");
   constexpr int NVP = Interleave<M::NV>::NVP;
   constexpr int NV = M::NV;
@@ -631,37 +631,73 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         constexpr int CW = G::RW + 3, EW = G::RW + 1, H = G::RH;
         constexpr int CB_BEG = G::R_BEG - 2, E_BEG = G::R_BEG - 1;
         constexpr double DZ = 0.85 - 0.75;
-        T* s_cb = sm + S::CB_OFF;
-        for (int e = tid; e < CW * H; e += nth) {
-          const int row = e / CW, col = e % CW;
-          const int y = rs_(s0 + CB_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
-          auto P = [&](int x) -> T { return wv(PP, x, rt); };
-          const T dp1 = P(rs_(y + 1)) - P(rs_(y - 1));
+        // chi_bar of one column from the pressures at y-2..y+2 and the normal velocities
+        // at y-1, y+1; dp1 = P(y+1) - P(y-1)
+        auto chi_bar = [&](T pm2, T pm1, T pp1, T pp2, T vm1, T vp1, T dp1) -> T {
           // only strong, compressive pressure jumps are flattened (Colella & Woodward 1984, A.1);
           // elsewhere chi_bar = 1 and z is not needed
-          const bool not_compressive = (wv(PN, rs_(y - 1), rt) - wv(PN, rs_(y + 1), rt)) <= T(0);
-          const bool weak = dvd(abs_(dp1), npmin(P(rs_(y + 1)), P(rs_(y - 1)))) <= T(.33);
+          const bool not_compressive = (vm1 - vp1) <= T(0);
+          const bool weak = dvd(abs_(dp1), npmin(pp1, pm1)) <= T(.33);
           T cb = T(1);
           if (!(not_compressive || weak)) {
-            const T dp2 = P(rs_(y + 2)) - P(rs_(y - 2));
+            const T dp2 = pp2 - pm2;
             const T z = dvd(abs_(dp1), abs_(dp2));
             cb = T(1) - dvd(z - T(.75), T(DZ));
             if (z > T(.85)) cb = T(0);
             if (z < T(.75)) cb = T(1);
           }
-          s_cb[row * CW + col] = cb;
-        }
-        __syncthreads();
-        for (int e = tid; e < EW * H; e += nth) {
-          const int row = e / EW, col = e % EW;
-          const int x = rs_(s0 + E_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
-          const T* cbrow = s_cb + row * CW - (s0 + CB_BEG);
-          const T cb = cbrow[x];
-          const T sgn = npsign(wv(PP, rs_(x + 1), rt) - wv(PP, rs_(x - 1), rt));
-          T chi = cb;
-          if (sgn < T(0)) chi = npmin(cb, cbrow[rs_(x + 1)]);
-          if (sgn > T(0)) chi = npmin(cb, cbrow[rs_(x - 1)]);
-          s_eta[row * EW + col] = chi;
+          return cb;
+        };
+        constexpr int FK = 4;  // eta columns per thread on tiles without a boundary map
+        if constexpr (DIM == 2 && !CL && EW % FK == 0) {
+          // one thread per strip of FK eta columns of a row: the chi_bar values it needs and
+          // the pressure differences eta's sign shares with them stay in registers
+          constexpr int NSF = EW / FK;
+          for (int e = tid; e < NSF * H; e += nth) {
+            const int strip = e / H, row = e % H;
+            const int rt = t0 - G::RT + row, x0 = s0 + E_BEG + strip * FK;
+            T P[FK + 6], V[FK + 4];  // P at x0-3 .. x0+FK+2, V at x0-2 .. x0+FK+1
+#pragma unroll
+            for (int i = 0; i < FK + 6; ++i) P[i] = wv(PP, x0 - 3 + i, rt);
+#pragma unroll
+            for (int i = 0; i < FK + 4; ++i) V[i] = wv(PN, x0 - 2 + i, rt);
+            T cb[FK + 2], dp[FK + 2];  // at x0-1 .. x0+FK
+#pragma unroll
+            for (int i = 0; i < FK + 2; ++i) {
+              dp[i] = P[i + 3] - P[i + 1];
+              cb[i] = chi_bar(P[i], P[i + 1], P[i + 3], P[i + 4], V[i], V[i + 2], dp[i]);
+            }
+#pragma unroll
+            for (int k = 0; k < FK; ++k) {
+              const T sgn = npsign(dp[k + 1]);
+              T chi = cb[k + 1];
+              if (sgn < T(0)) chi = npmin(cb[k + 1], cb[k + 2]);
+              if (sgn > T(0)) chi = npmin(cb[k + 1], cb[k]);
+              s_eta[row * EW + strip * FK + k] = chi;
+            }
+          }
+        } else {
+          T* s_cb = sm + S::CB_OFF;
+          for (int e = tid; e < CW * H; e += nth) {
+            const int row = e / CW, col = e % CW;
+            const int y = rs_(s0 + CB_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
+            auto P = [&](int x) -> T { return wv(PP, x, rt); };
+            const T dp1 = P(rs_(y + 1)) - P(rs_(y - 1));
+            s_cb[row * CW + col] = chi_bar(P(rs_(y - 2)), P(rs_(y - 1)), P(rs_(y + 1)), P(rs_(y + 2)),
+                                           wv(PN, rs_(y - 1), rt), wv(PN, rs_(y + 1), rt), dp1);
+          }
+          __syncthreads();
+          for (int e = tid; e < EW * H; e += nth) {
+            const int row = e / EW, col = e % EW;
+            const int x = rs_(s0 + E_BEG + col), rt = DIM == 2 ? rt_(t0 - G::RT + row) : 0;
+            const T* cbrow = s_cb + row * CW - (s0 + CB_BEG);
+            const T cb = cbrow[x];
+            const T sgn = npsign(wv(PP, rs_(x + 1), rt) - wv(PP, rs_(x - 1), rt));
+            T chi = cb;
+            if (sgn < T(0)) chi = npmin(cb, cbrow[rs_(x + 1)]);
+            if (sgn > T(0)) chi = npmin(cb, cbrow[rs_(x - 1)]);
+            s_eta[row * EW + col] = chi;
+          }
         }
       }
       if (a.viscosity) {
@@ -687,20 +723,23 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
             const T cmin = npmin(cs_x, cs_xp);
             nu = npmin(T(1), dvd(lam * lam, a.av_beta * (cmin * cmin))) * lam;
           }
+          T mu[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) mu[i] = T(0);
           if constexpr (WSIN) {
             // x, xp lie in [s0-1, s0+TS] and rt in [t0, t0+TT) (clamped or not): the staged strip
             if (strip_tma) {
               using SB = StripBox<T, AX, TS, TT>;
 #pragma unroll
               for (int v = 0; v < NV; ++v)
-                s_mu[(row * W + col) * NVP + v] =
+                mu[M::var(v)] =
                     a.av_alpha * (nu * (qs_box[SB::at(v, xp, rt, s0, t0)] - qs_box[SB::at(v, x, rt, s0, t0)]));
             } else {
               const T* qrow = sm + S::QS_OFF + (rt - t0) * S::QSW - (s0 - 1);
 #pragma unroll
               for (int v = 0; v < NV; ++v) {
                 const T* qv = qrow + v * TT * S::QSW;
-                s_mu[(row * W + col) * NVP + v] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+                mu[M::var(v)] = a.av_alpha * (nu * (qv[xp] - qv[x]));
               }
             }
           } else {
@@ -708,9 +747,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
               const T* qv = qrow + v * G::QH * G::QW;
-              s_mu[(row * W + col) * NVP + v] = a.av_alpha * (nu * (qv[xp] - qv[x]));
+              mu[M::var(v)] = a.av_alpha * (nu * (qv[xp] - qv[x]));
             }
           }
+          store_aos<M>(s_mu, row * W + col, mu);
         }
       }
       __syncthreads();
@@ -878,8 +918,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       solve(e, 0, wSr, wp, wm, qp, qm, fp, fm, F);
       if constexpr (SCH == PPM) {
         if (a.viscosity) {
+          T mu[8];
+          load_aos<M>(s_mu, e, mu);
 #pragma unroll
-          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + s_mu[e * NVP + v];
+          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + mu[M::var(v)];
         }
       }
       store_aos<M>(s_F, e, F);
@@ -945,8 +987,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       if constexpr (SCH == PPM) {
         // the viscous flux of this interface sits where F goes: read it, then overwrite
         if (a.viscosity) {
+          T mu[8];
+          load_aos<M>(s_mu, row * W + col, mu);
 #pragma unroll
-          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + s_mu[(row * W + col) * NVP + v];
+          for (int v = 0; v < NV; ++v) F[M::var(v)] = F[M::var(v)] + mu[M::var(v)];
         }
       }
       store_aos<M>(s_F, row * W + col, F);

@@ -227,18 +227,28 @@ __device__ __forceinline__ void hllc(int label, int physical, T gamma, const T* 
   T uL, uR;
   if constexpr (M::VY) { uL = label == 0 ? wm[1] : wm[2]; uR = label == 0 ? wp[1] : wp[2]; }
   else { uL = wm[1]; uR = wp[1]; }
-  const T cL = sqrt_(gamma * dvd(pL, rL)), cR = sqrt_(gamma * dvd(pR, rR));
-  const T sqL = sqrt_(rL), sqR = sqrt_(rR);
-  T u_hat, c2_hat;
+  T cL, cR, sqL, sqR, u_hat, c2_hat;
   if constexpr (Prec<T>::EXACT) {
+    cL = sqrt_(gamma * dvd(pL, rL));
+    cR = sqrt_(gamma * dvd(pR, rR));
+    sqL = sqrt_(rL);
+    sqR = sqrt_(rR);
     u_hat = dvd(uL * sqL + uR * sqR, sqL + sqR);
     c2_hat = dvd(sqL * (cL * cL) + sqR * (cR * cR), sqL + sqR)
            + (T(.5) * ((uR - uL) * (uR - uL))) * dvd(sqL * sqR, (sqL + sqR) * (sqL + sqR));
   } else {
-    // FP32: one reciprocal of the weight sum for the three Roe-weighted terms
+    // FP32: one reciprocal square root per density gives its square root (the Roe weight)
+    // and, times sqrt(gamma p), the sound speed; sqrt(rho) c^2 = gamma p / sqrt(rho).  A zero
+    // density has weight and sound speed 0, as sqrt(0) and the masked divide give.  One
+    // reciprocal of the weight sum serves the three Roe-weighted terms.
+    const T iL = rL == T(0) ? T(0) : rsqrtf(rL), iR = rR == T(0) ? T(0) : rsqrtf(rR);
+    sqL = rL * iL;
+    sqR = rR * iR;
+    cL = sqrt_(gamma * pL) * iL;
+    cR = sqrt_(gamma * pR) * iR;
     const T sw = sqL + sqR, inv = sw != T(0) ? T(1) / sw : T(0);
     u_hat = (uL * sqL + uR * sqR) * inv;
-    c2_hat = (sqL * (cL * cL) + sqR * (cR * cR)) * inv + (T(.5) * ((uR - uL) * (uR - uL))) * ((sqL * sqR) * (inv * inv));
+    c2_hat = (gamma * (pL * iL + pR * iR)) * inv + (T(.5) * ((uR - uL) * (uR - uL))) * ((sqL * sqR) * (inv * inv));
   }
   const T ch = sqrt_(c2_hat);
   const T sL = npmin(uL - cL, u_hat - ch);

@@ -223,7 +223,10 @@ template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Sm
   // the face arrays reuse the q level once it is dead; PCM reads raw q on faces, so it keeps q
   static constexpr int FA_OFF = SCH == PCM ? n_q : 0;
   static constexpr int n_region0 = ceil_to((n_q + n_qw) > (FA_OFF + n_face + n_F) ? (n_q + n_qw) : (FA_OFF + n_face + n_F), 4);
-  static constexpr int n_w = ceil_to(NV * G::WH * G::WW, 4);
+  // WSIN tiles of axis-0 sweeps read the w level where its bulk copy lands: room for that box
+  // (at most WH + 3 elements across, rounded to 16 bytes) and 128 bytes of alignment
+  static constexpr int n_w_box = (WSIN && DIM == 2) ? NV * G::WW * ceil_to(G::WH + 3, 4) + 32 : 0;
+  static constexpr int n_w = ceil_to(NV * G::WH * G::WW > n_w_box ? NV * G::WH * G::WW : n_w_box, 4);
   static constexpr int n_R = 2 * NVP * G::RH * G::RW;
   static constexpr int n_lam = G::FH * G::YW;
   static constexpr int base = ceil_to(n_region0 + n_w + n_R + n_lam + 64, 4);
@@ -251,6 +254,17 @@ template <int SCH, int DIM, int TS, int TT, int NV, bool WSIN = false> struct Sm
   static constexpr bool QS_IN_GAP = ETA_IN_GAP && (n_q + n_qw + n_eta + n_cb + n_qs <= FA_OFF + n_face);
   static constexpr int QS_OFF = QS_IN_GAP ? CB_OFF + n_cb : total0;
   static constexpr int total = total0 + (QS_IN_GAP ? 0 : n_qs);
+};
+
+// Addressing of the w level: element (plane pl, row r, column c), rows and columns counted
+// from the level's first, at pl * PS + r * PR + c * PC.  A plane per variable with rows along
+// the sweep, or (IN_BOX) the axis-0 bulk-copy box as it lands: the box's x runs across the
+// sweep, so rows are contiguous there.
+template <bool IN_BOX, class G, class B> struct WLayout {
+  static constexpr int PS = G::WH * G::WW, PR = G::WW, PC = 1;
+};
+template <class G, class B> struct WLayout<true, G, B> {
+  static constexpr int PS = B::BH * B::BW, PR = 1, PC = B::BW;
 };
 
 template <class M, typename T> __device__ __forceinline__ void load_sm(const T* base, int stride, int idx, T* x) {
@@ -365,6 +379,14 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   T* s_F = s_fa + S::n_face;
   T* s_w = sm + S::n_region0;
   T* s_R = s_w + S::n_w;
+  // the w level: planar at s_w, or (axis-0 sweeps staged by bulk copy) the copied box itself
+  constexpr bool W_IN_BOX = WSIN && TMA && DIM == 2 && AX == 0;
+  using WL = WLayout<W_IN_BOX, G, TmaBox<T, SCH, 2, 0, TS, TT, M::NV>>;
+  T* s_wb = s_w;
+  // element (plane pl, real row rt, real column x) of the w level
+  auto wat = [&](int pl, int rt, int x) -> T {
+    return s_wb[pl * WL::PS + (rt - (t0 - G::WT)) * WL::PR + (x - (s0 + G::W_BEG)) * WL::PC];
+  };
   T* s_lam = s_R + S::n_R;
 
   const int Ns = DIM == 1 ? a.n0 : (AX == 0 ? a.n0 : a.n1);
@@ -443,7 +465,9 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       using B = TmaBox<T, SCH, DIM, AX, TS, TT, NV>;
       using SB = StripBox<T, AX, TS, TT>;
       __shared__ unsigned long long s_bar;
-      T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_R) + 127) & ~uintptr_t(127));
+      // axis 0: the box lands in the w level's region and is read in place; axis 1: it lands
+      // in the (still unused) R region and is copied into the planar w level
+      T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(AX == 0 ? s_w : s_R) + 127) & ~uintptr_t(127));
       if (tid == 0) {
         mbar_init(&s_bar, 1);
         mbar_fence_init();
@@ -469,13 +493,17 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         return;
       }
       const int xo = B::xoff(t0);
-      for (int e = tid; e < W * H; e += nth) {
-        int row, col;
-        if (AX == 0) { row = e % H; col = e / H; } else { col = e % W; row = e / W; }
-#pragma unroll
-        for (int s = 0; s < NV; ++s)
-          s_w[(s * H + row) * W + col] = AX == 1 ? stage[(s * B::BH + row) * B::BW + col + xo]
-                                                 : stage[(s * B::BH + col) * B::BW + row + xo];
+      if constexpr (AX == 0) {
+        s_wb = stage + xo;
+      } else {
+        // one warp per (plane, row), its lanes along the row
+        const int lane = tid & 31;
+        for (int p = tid >> 5; p < NV * H; p += nth / 32) {
+          const int s = p / H, row = p % H;
+          const T* src = stage + (s * B::BH + row) * B::BW + xo;
+          T* dst = s_w + (s * H + row) * W;
+          for (int col = lane; col < W; col += 32) dst[col] = src[col];
+        }
       }
     } else {
       for (int e = tid; e < W * H; e += nth) {
@@ -622,9 +650,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       constexpr int PN = plane_of<M>(1 + (DIM == 1 ? 0 : AX));
       constexpr int PT = DIM == 2 ? plane_of<M>(1 + (1 - AX)) : 0;
       // w level at real column x and real row rt
-      auto wv = [&](int pl, int x, int rt) -> T {
-        return s_w[(pl * G::WH + (rt - (t0 - G::WT))) * G::WW + (x - (s0 + G::W_BEG))];
-      };
+      auto wv = [&](int pl, int x, int rt) -> T { return wat(pl, rt, x); };
       if (a.flatten) {
         // chi_bar on columns [s0-3, s0+TS+3), then eta on [s0-2, s0+TS+2) from it; each
         // intermediate is served at a virtual index by its value at the mapped index
@@ -763,15 +789,16 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     constexpr int K = PpmStrip<G::RW, DIM>::K, NS = G::RW / K;
     constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
     for (int e = tid; e < NS * H * NV; e += nth) {
-      // strip-major order: a warp's threads sit on consecutive rows (fewer bank conflicts)
+      // strip-major order, the variables of a cell on consecutive threads: a warp's scalar
+      // stores into the cell-interleaved level hit distinct banks
       const int strip = e / (NV * H), rem = e % (NV * H);
-      const int s = rem / H, row = rem % H, col0 = strip * K;
+      const int s = rem % NV, row = rem / NV, col0 = strip * K;
       const int vs0 = s0 + G::R_BEG + col0, vt = t0 - G::RT + row;
-      const T* wrow = s_w + (s * WH + row + (G::WT - G::RT)) * WW - (s0 + G::W_BEG);
+      const T* wrow = s_wb + s * WL::PS + (row + (G::WT - G::RT)) * WL::PR - (s0 + G::W_BEG) * WL::PC;
       T* rl = s_R + (row * W + col0) * NVP + s;
       T* rr = rl + NVP * H * W;
       const T* erow = a.flatten ? s_eta + row * (W + 1) - (s0 + G::R_BEG - 1) : nullptr;
-      recon_ppm_strip<T, K>([&](int x) -> T { return wrow[x]; }, vs0, [&](int k, T wl, T wr, T fr) {
+      recon_ppm_strip<T, K>([&](int x) -> T { return wrow[x * WL::PC]; }, vs0, [&](int k, T wl, T wr, T fr) {
         rl[k * NVP] = wl;
         rr[k * NVP] = wr;
         const int vs = vs0 + k;
@@ -786,8 +813,8 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       const int row = rem / W, col = rem % W;
       const int vs = s0 + G::R_BEG + col, vt = t0 - G::RT + row;
       const int rs = rs_(vs), rt = DIM == 2 ? rt_(vt) : 0;
-      const T* wrow = s_w + (s * WH + (rt - (t0 - G::WT))) * WW - (s0 + G::W_BEG);
-      auto at = [&](int x) -> T { return wrow[x]; };
+      const T* wrow = s_wb + s * WL::PS + (rt - (t0 - G::WT)) * WL::PR - (s0 + G::W_BEG) * WL::PC;
+      auto at = [&](int x) -> T { return wrow[x * WL::PC]; };
       const T* erow = (SCH == PPM && a.flatten) ? s_eta + row * (W + 1) - (s0 + G::R_BEG - 1) : nullptr;
       T wl, wr;
       reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr, erow);
@@ -863,7 +890,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     }
   };
   auto load_wS = [&](int x, int rt, T* out) {
-    load_sm<M>(s_w, G::WH * G::WW, (rt - (t0 - G::WT)) * G::WW + (x - (s0 + G::W_BEG)), out);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = T(0);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) out[M::var(v)] = wat(v, rt, x);
   };
   // face states of interface vk at real row rt
   auto face_states = [&](int vk, int rt, T* wp, T* wm) {
@@ -1060,7 +1090,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs<T>& a, const int s0, 
   const int Nt = DIM == 1 ? 1 : (AX == 0 ? a.n1 : a.n0);
   if constexpr (TMA_OK && DIM == 2 && (WSIN || !G::HO)) {
     using B = TmaBox<T, SCH, DIM, AX, TS, TT, Model<MID>::NV>;
-    if constexpr ((size_t)S::n_R * sizeof(T) >= (size_t)B::BYTES + 128) {
+    if constexpr ((size_t)(AX == 0 ? S::n_w : S::n_R) * sizeof(T) >= (size_t)B::BYTES + 128) {
       const bool box_in = a.tmaps != nullptr && B::inside(s0, t0, a.n0, a.n1);
       if (box_in) {
         sweep_tile_body<T, MID, SCH, SOL, DIM, AX, TS, TT, false, NT, true, WSIN>(a, s0, t0, smem_raw);

@@ -46,6 +46,21 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
   return done != 0;
 }
 
+// the same test, letting the thread sleep up to ``hint_ns`` nanoseconds for the phase to complete
+__device__ __forceinline__ bool mbar_try_wait_sleep(unsigned long long* bar, unsigned parity, unsigned hint_ns) {
+  unsigned done;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return done != 0;
+}
+
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -53,16 +68,19 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 }
 
 // wait for phase ``parity`` of the barrier for at most ``limit_ns`` nanoseconds of wall
-// time (and at most 2^24 polls); false if the limit ran out
+// time (and at most 2^22 polls, each sleeping at most 20 us); false if the limit ran out.
+// The polling thread sleeps in the barrier test instead of spinning, which leaves the
+// issue slots to the other warps on the SM.
 constexpr unsigned long long kCopyWaitNs = 2000000ull;      // a tile's bulk copy: 2 ms (it takes microseconds)
 constexpr unsigned long long kDrainWaitNs = 50000000ull;    // after a timeout, for the copy in flight: 50 ms
+constexpr unsigned kPollSleepNs = 20000u;
 __device__ __forceinline__ bool mbar_wait_timed(unsigned long long* bar, unsigned parity,
                                                 unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = globaltimer_ns();
-  for (int i = 0; i < (1 << 24); ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 15) == 15 && globaltimer_ns() - t0 > limit_ns) return false;
+  for (int i = 0; i < (1 << 22); ++i) {
+    if (mbar_try_wait_sleep(bar, parity, kPollSleepNs)) return true;
+    if (globaltimer_ns() - t0 > limit_ns) return false;
   }
   return false;
 }

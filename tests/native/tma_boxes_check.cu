@@ -38,6 +38,17 @@ template <typename T, int SCH, int AX, int TS, int TT> bool check_grid(int n0, i
         // and those are the tile's virtual cells [s0+W_BEG, s0+TS+W_END) x [t0-WT, t0+TT+WT)
         if (AX == 1) REQUIRE(x + xo == s0 + G::W_BEG);
         else REQUIRE(x + xo == t0 - G::WT);
+        // axis 0 reads the level in place (WLayout<true>): element (row r, column c) of the
+        // level is grid cell (s0 + W_BEG + c, t0 - WT + r) of the box
+        if (AX == 0) {
+          using WL = WLayout<true, G, B>;
+          for (int c = 0; c < G::WW; ++c)
+            for (int r = 0; r < G::WH; ++r) {
+              const int e = r * WL::PR + c * WL::PC + xo;
+              REQUIRE(e >= 0 && e < B::BW * B::BH);
+              REQUIRE(x + e % B::BW == t0 - G::WT + r && y + e / B::BW == s0 + G::W_BEG + c);
+            }
+        }
       }
       if (SCH == PPM && SB::inside(s0, t0, n0, n1)) {
         ++g_checked;
@@ -65,6 +76,18 @@ template <typename T, int SCH, int AX, int TS, int TT> bool check_all() {
     if (!check_grid<T, SCH, AX, TS, TT>(sz[0], sz[1])) return false;
   return true;
 }
+
+// the axis-0 box of NV planes, aligned up to 128 bytes, fits the w level's region of the WSIN tiles
+template <typename T, int SCH, int TS, int TT, int NV> constexpr bool box_fits_w() {
+  return SCH < PPM || (size_t)Smem<SCH, 2, TS, TT, NV, true>::n_w * sizeof(T) >=
+                          (size_t)TmaBox<T, SCH, 2, 0, TS, TT, NV>::BYTES + 128;
+}
+static_assert(box_fits_w<float, PPM, 32, 8, 4>() && box_fits_w<float, PPM, 32, 15, 4>() &&
+                  box_fits_w<float, PPM, 32, 8, 8>() && box_fits_w<double, PPM, 32, 8, 4>() &&
+                  box_fits_w<double, PPM, 32, 15, 4>() && box_fits_w<double, PPM, 32, 8, 8>() &&
+                  box_fits_w<float, WENO5, 32, 8, 8>() && box_fits_w<double, WENO5, 32, 8, 8>() &&
+                  box_fits_w<float, WENO7, 32, 15, 4>() && box_fits_w<double, WENO7, 32, 15, 4>(),
+              "axis-0 bulk-copy box exceeds the w level");
 
 template <typename T, int SCH> bool check_scheme() {
   return check_all<T, SCH, 0, 32, 8>() && check_all<T, SCH, 1, 32, 8>() && check_all<T, SCH, 0, 32, 15>() &&

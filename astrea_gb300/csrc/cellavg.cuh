@@ -21,28 +21,12 @@ namespace astrea {
 // One warp per strip of 30 columns x TY rows: its 32 lanes sit on 32
 // consecutive columns (lanes 0 and 31 are the strip's halo) and walk down the
 // rows, keeping rows i-1, i, i+1 (state and point primitives) in registers and
-// taking the axis-1 neighbours from the adjacent lanes.  The rows of the state
-// arrive by asynchronous copies (cp.async) into a per-warp ring of RING rows in
-// shared memory, issued RING rows before their use, so that many loads per warp
-// are in flight without holding registers.  Each lane copies and reads only its
-// own column: no block barriers.
+// taking the axis-1 neighbours from the adjacent lanes; each row's state is
+// loaded two rows before it is converted.  No shared memory, no block barriers.
 constexpr int CA_W = 30, CA_NT = 256, CA_WARPS = CA_NT / 32;
 template <typename T, int MID> struct CellAvgTile {
   static constexpr int TY = 16;  // rows per strip
-  static constexpr int ROW_BYTES = Model<MID>::NV * 32 * (int)sizeof(T);  // one row of a warp's ring
-  // ring depth: at most 8 rows, at most 48 KB of static shared memory per block
-  static constexpr int RING = (48 * 1024) / (CA_WARPS * ROW_BYTES) >= 8 ? 8 : (48 * 1024) / (CA_WARPS * ROW_BYTES);
-  static_assert(RING >= 3, "cell-average ring too shallow");
 };
-
-// asynchronous element copy global -> shared (4 or 8 bytes), completion by commit groups
-template <typename T> __device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
-  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-  if constexpr (sizeof(T) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
-  else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // The FP64 kernels write both sweep orders (bit-level parity); the FP32 ones
 // write the axis-0 order only, which both FP32 sweeps read (its rounding differs
@@ -66,43 +50,42 @@ __device__ __forceinline__ void cell_average_strip(const T* __restrict__ q, T* _
     const int gi = (i >= 0 && i < n0) ? i : bc_map(i, n0, bc);
     return q + (long long)gi * n1 + gj;
   };
-  // this warp's ring: row slot k, plane s, lane at ((k * NV) + s) * 32 + lane
-  constexpr int RING = CellAvgTile<T, MID>::RING;
-  __shared__ T ring_all[CA_WARPS * RING * NV * 32];
-  T* ring = ring_all + (threadIdx.x >> 5) * (RING * NV * 32) + lane;
-  // rows k = 0 .. TY+1 of the strip are i0-1 .. i0+TY; row k goes to slot k % RING, one
-  // commit group per row (empty past the strip's last row).  RING-1 rows are in flight:
-  // reading row k waits until at most RING-2 groups are pending, then row k+RING-1 is
-  // issued into the slot of row k-1, which the previous read emptied.
-  auto issue = [&](int k) {
-    if (k < TY + 2) {
-      const T* p = row_ptr(i0 - 1 + k);
-      T* d = ring + (k % RING) * NV * 32;
+  auto expand = [&](const T* v, T* x) {
 #pragma unroll
-      for (int s = 0; s < NV; ++s) cp_async_elem(d + s * 32, p + s * plane);
+    for (int k = 0; k < 8; ++k) x[k] = T(0);
+#pragma unroll
+    for (int s = 0; s < NV; ++s) x[M::var(s)] = v[s];
+  };
+  T qm[8], q0[8], qp[8], wm[8], w0[8], wp[8], nxt[NV], nxt2[NV];  // nxt: row i+1, nxt2: row i+2
+  {
+    const T* pm = row_ptr(i0 - 1);
+    const T* p0 = row_ptr(i0);
+    const T* p1 = row_ptr(i0 + 1);
+    const T* p2 = row_ptr(i0 + 2);
+    T a[NV], b[NV];
+#pragma unroll
+    for (int s = 0; s < NV; ++s) {
+      a[s] = pm[s * plane];
+      b[s] = p0[s * plane];
+      nxt[s] = p1[s * plane];
+      nxt2[s] = p2[s * plane];
     }
-    cp_async_commit();
-  };
-  auto take = [&](int k, T* x) {  // row k (its copy complete) into the 8-variable layout
-    cp_async_wait<RING - 2>();
-    const T* d = ring + (k % RING) * NV * 32;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) x[i] = T(0);
-#pragma unroll
-    for (int s = 0; s < NV; ++s) x[M::var(s)] = d[s * 32];
-    issue(k + RING - 1);
-  };
-#pragma unroll
-  for (int k = 0; k < RING - 1; ++k) issue(k);
-  T qm[8], q0[8], qp[8], wm[8], w0[8], wp[8];
-  take(0, qm);
-  take(1, q0);
-  c2p<M>(qm, wm, gm1);
-  c2p<M>(q0, w0, gm1);
+    expand(a, qm);
+    expand(b, q0);
+    c2p<M>(qm, wm, gm1);
+    c2p<M>(q0, w0, gm1);
+  }
   for (int r = 0; r < TY; ++r) {
     const int i = i0 + r;
     if (i >= n0) break;  // whole warp
-    take(r + 2, qp);
+    expand(nxt, qp);
+#pragma unroll
+    for (int s = 0; s < NV; ++s) nxt[s] = nxt2[s];
+    if (r + 2 < TY) {  // row i+3, two rows ahead of its use
+      const T* pn = row_ptr(i + 3);
+#pragma unroll
+      for (int s = 0; s < NV; ++s) nxt2[s] = pn[s * plane];
+    }
     c2p<M>(qp, wp, gm1);
     // axis-1 neighbours from the adjacent lanes
     T ql[8], qr[8], wl[8], wr[8];
@@ -161,7 +144,6 @@ __device__ __forceinline__ void cell_average_strip(const T* __restrict__ q, T* _
       wm[k] = w0[k]; w0[k] = wp[k];
     }
   }
-  cp_async_wait<0>();  // no copy outlives the strip
 }
 
 template <typename T, int MID>

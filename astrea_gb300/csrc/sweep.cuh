@@ -436,7 +436,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     using SB = StripBox<T, AX, TS, TT>;
     static_assert(NV * SB::BH * SB::BW + 128 / (int)sizeof(T) <= S::n_qs, "viscous strip box exceeds its region");
     strip_tma = a.viscosity && a.qmaps != nullptr && SB::inside(s0, t0, a.n0, a.n1);
-    qs_box = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(sm + S::QS_OFF) + 127) & ~uintptr_t(127));
+    qs_box = align128_shared(sm + S::QS_OFF);
   }
 
   if constexpr (WSIN) {
@@ -467,7 +467,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       __shared__ unsigned long long s_bar;
       // axis 0: the box lands in the w level's region and is read in place; axis 1: it lands
       // in the (still unused) R region and is copied into the planar w level
-      T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(AX == 0 ? s_w : s_R) + 127) & ~uintptr_t(127));
+      T* stage = align128_shared(AX == 0 ? s_w : s_R);
       if (tid == 0) {
         mbar_init(&s_bar, 1);
         mbar_fence_init();
@@ -496,13 +496,10 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       if constexpr (AX == 0) {
         s_wb = stage + xo;
       } else {
-        // one warp per (plane, row), its lanes along the row
-        const int lane = tid & 31;
-        for (int p = tid >> 5; p < NV * H; p += nth / 32) {
-          const int s = p / H, row = p % H;
-          const T* src = stage + (s * B::BH + row) * B::BW + xo;
-          T* dst = s_w + (s * H + row) * W;
-          for (int col = lane; col < W; col += 32) dst[col] = src[col];
+        for (int e = tid; e < W * H; e += nth) {
+          const int col = e % W, row = e / W;
+#pragma unroll
+          for (int s = 0; s < NV; ++s) s_w[(s * H + row) * W + col] = stage[(s * B::BH + row) * B::BW + col + xo];
         }
       }
     } else {
@@ -520,7 +517,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     // one thread issues the bulk copy of the whole box into the (still unused) R region
     using B = TmaBox<T, SCH, DIM, AX, TS, TT, NV>;
     __shared__ unsigned long long s_bar;
-    T* stage = reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(s_R) + 127) & ~uintptr_t(127));
+    T* stage = align128_shared(s_R);
     if (tid == 0) {
       mbar_init(&s_bar, 1);
       mbar_fence_init();
@@ -802,8 +799,11 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         rl[k * NVP] = wl;
         rr[k * NVP] = wr;
         const int vs = vs0 + k;
-        if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt)
-          a.wface_out[M::var(s) * a.plane + gidx(vs, vt)] = fr;
+        // face values for the constrained transport (2D MHD grids only)
+        if constexpr (M::MHD) {
+          if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt)
+            a.wface_out[M::var(s) * a.plane + gidx(vs, vt)] = fr;
+        }
       }, erow);
     }
   } else {
@@ -820,7 +820,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       reconstruct<SCH, T>(at, rs_, rs, a.limiter, wl, wr, erow);
       s_R[(row * W + col) * NVP + s] = wl;
       s_R[NVP * H * W + (row * W + col) * NVP + s] = wr;
-      if (a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) {
+      if (M::MHD && a.wface_out && vs >= s0 && vs < s0 + TS && vs < Ns && vt >= t0 && vt < t0 + TT && vt < Nt) {
         // the face value the constrained transport uses: PPM's unlimited 4th-order
         // face (ppm.py:38-42), the right face value of the other schemes (weno.py:168, plm.py:39)
         T fv;

@@ -19,6 +19,13 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
 
+// p moved up to the next 128-byte boundary of the shared window, by pointer arithmetic on p
+// (which keeps the pointer known to the compiler as shared, so its accesses stay shared loads)
+template <typename T> __device__ __forceinline__ T* align128_shared(T* p) {
+  const unsigned mis = smem_u32(p) & 127u;
+  return p + (mis ? (128u - mis) / sizeof(T) : 0u);
+}
+
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }

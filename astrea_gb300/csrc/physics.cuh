@@ -172,11 +172,21 @@ template <class M, typename T> __device__ __forceinline__ void roe_avg(const T* 
   const T rm = sqrt_(wm[0]), rp = sqrt_(wp[0]);
   const T den = rm + rp;
   y[0] = rm * rp;
+  if constexpr (Prec<T>::EXACT) {
 #pragma unroll
-  for (int i = 1; i < 4; ++i) y[i] = dvd(wp[i] * rp + wm[i] * rm, den);
-  y[4] = dvd(rp * wp[4] + rm * wm[4], den);
+    for (int i = 1; i < 4; ++i) y[i] = dvd(wp[i] * rp + wm[i] * rm, den);
+    y[4] = dvd(rp * wp[4] + rm * wm[4], den);
 #pragma unroll
-  for (int i = 5; i < 8; ++i) y[i] = M::MHD ? dvd(wp[i] * rm + wm[i] * rp, den) : T(0);
+    for (int i = 5; i < 8; ++i) y[i] = M::MHD ? dvd(wp[i] * rm + wm[i] * rp, den) : T(0);
+  } else {
+    // FP32: one reciprocal of the weight sum
+    const T inv = den != T(0) ? T(1) / den : T(0);
+#pragma unroll
+    for (int i = 1; i < 4; ++i) y[i] = (wp[i] * rp + wm[i] * rm) * inv;
+    y[4] = (rp * wp[4] + rm * wm[4]) * inv;
+#pragma unroll
+    for (int i = 5; i < 8; ++i) y[i] = M::MHD ? (wp[i] * rm + wm[i] * rp) * inv : T(0);
+  }
 }
 
 // ---------------------------------------------------------------- wave speed
@@ -193,9 +203,12 @@ template <class M, int AX, typename T> __device__ __forceinline__ T max_speed(co
     const T s = a2 + b2;
     const T cf2 = T(.5) * (s + sqrt_(s * s - (T(4) * a2) * bn2));
     fast = abs_(vn) + sqrt_(cf2);
-  } else {
+  } else if constexpr (Prec<T>::EXACT) {
     const T cf2 = T(.5) * (a2 + sqrt_(a2 * a2));
     fast = abs_(vn) + sqrt_(cf2);
+  } else {
+    // FP32: for a2 >= 0, (a2 + sqrt(a2^2)) / 2 is a2 itself (a2 < 0 is handled below)
+    fast = abs_(vn) + sqrt_(a2);
   }
   if (a2 < T(0)) {
     T c = sqrt_(vn * vn - a2);

@@ -1047,6 +1047,9 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   {
     constexpr int W = G::KW;
     const T dxT = T(a.dx);
+    // FP32 multiplies by the reciprocal of dx, formed in FP32 (FP64 divides, as the reference does)
+    T rdx = T(0);
+    if constexpr (!Prec<T>::EXACT) rdx = __frcp_rn(dxT);
     const T dtT = T(a.clock->dt);
     for (int e = tid; e < TS * TT; e += nth) {
       int row, col;
@@ -1059,7 +1062,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       load_aos<M>(s_F, row * W + col, Fl);
 #pragma unroll
       for (int s = 0; s < NV; ++s) {
-        const T D = (Fr[M::var(s)] - Fl[M::var(s)]) / dxT;
+        const T D = Prec<T>::EXACT ? (Fr[M::var(s)] - Fl[M::var(s)]) / dxT : (Fr[M::var(s)] - Fl[M::var(s)]) * rdx;
         if (a.mode == 0) {
           a.dout[s * a.plane + g] = D;
         } else {

@@ -124,7 +124,8 @@ struct IEngine {
 // Sweep-tile autotuner: per (precision, model, scheme, solver, flags, grid size,
 // device, axis) the fastest candidate tile, timed once on the grid itself and
 // shared by every handle with the same key.  ASTREA_SWEEP_TILE=<index> forces a
-// candidate (where it is built).
+// candidate on both axes, ASTREA_SWEEP_TILE=<index>,<index> one per axis (where it
+// is built).
 static std::mutex g_tune_mutex;
 static std::map<std::string, int> g_tune_cache;
 
@@ -349,12 +350,18 @@ template <typename T> struct Engine final : IEngine {
     if (cs != cudaStreamCaptureStatusNone) return ASTREA_OK;  // keep the default tile inside a capture
     tuned = true;
     const char* env = std::getenv("ASTREA_SWEEP_TILE");
-    const int forced = (env && env[0] >= '0' && env[0] <= '9') ? std::atoi(env) : -1;
+    int forced_ax[2] = {-1, -1};
+    if (env && env[0] >= '0' && env[0] <= '9') {
+      forced_ax[0] = forced_ax[1] = std::atoi(env);
+      const char* comma = std::strchr(env, ',');
+      if (comma && comma[1] >= '0' && comma[1] <= '9') forced_ax[1] = std::atoi(comma + 1);
+    }
     int dev = 0;
     CK(cudaGetDevice(&dev));
     for (int ax = 0; ax < cfg.dim; ++ax) {
       int n_cand = 0;
       for (int t = 0; t < NTILES2; ++t) n_cand += cand[ax][t] != nullptr;
+      const int forced = forced_ax[ax];
       if (forced >= 0 && forced < NTILES2 && cand[ax][forced]) { tile[ax] = forced; sweep[ax] = cand[ax][forced]; continue; }
       if (n_cand < 2) continue;
       char key[160];

@@ -69,6 +69,14 @@ def test_both_tiles_give_the_same_update(boundary):
     assert close(a, b)
 
 
+def test_tile_forced_per_axis():
+    # ASTREA_SWEEP_TILE=<axis 0>,<axis 1>: the mix the tuner may pick gives the same update
+    a, ta = run(96, 32, 0)
+    b, tb = run(96, 32, "1,0")
+    assert tb == [(32, 15), (32, 8)]
+    assert close(a, b)
+
+
 def test_tuner_picks_a_built_tile():
     _, t32 = run(256, 32, None)
     assert all(t in [(32, 8), (32, 15)] for t in t32)

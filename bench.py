@@ -53,7 +53,7 @@ WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc) with flattening and ar
 # launch list (profiles/sweep_kernel_f32_ppm_hllc_2d.md); scaled by cells for
 # other sizes.  Slightly above the algorithmic bytes: the viscous strip reads
 # the stage state once more besides its cell averages.
-SWEEP_DRAM_BYTES = 220.6e6
+SWEEP_DRAM_BYTES = 223.1e6
 SWEEP_DRAM_CELLS = 2048 * 2048
 # Floating-point operations per cell-update of one SSPRK3 step (every kernel of the step),
 # from ncu's SASS op counters (fadd + fmul + 2 x ffma, and the FP64 counterparts) over one
@@ -67,7 +67,7 @@ FLOPS_FP64_PER_CELL_UPDATE = 11979.3
 # warp instructions per cell-update of the FP32 step (smsp__inst_executed.sum of every launch of a
 # step, launch list at 2048^2, profiles/sweep_kernel_f32_ppm_hllc_2d.md): against the issue rate of
 # one warp instruction per SM sub-partition per clock
-WARP_INSTR_FP32_PER_CELL_UPDATE = 364.6
+WARP_INSTR_FP32_PER_CELL_UPDATE = 331.0
 SMSP_PER_SM = 4
 # per-SM, per-clock issue rates of the FP32 and FP64 fused multiply-add pipes on GB300
 # (ncu: sm__sass_thread_inst_executed_op_{ffma,dfma}_pred_on.sum.peak_sustained / SMs)
@@ -397,10 +397,14 @@ def batched_fp64_check(cfgs, seeds, steps, count=32):
         torch.cuda.synchronize()
         out[prec] = ([b.planes(g)[0].double().clone() for g in range(len(sub))], b.clocks()["status"])
         del b
-    l1 = [float(torch.mean(torch.abs(a - d))) for a, d, st32, st64 in
-          zip(out[32][0], out[64][0], out[32][1], out[64][1]) if st32 == 0 and st64 == 0 and torch.isfinite(a).all()]
-    return {"instances": len(sub), "finite_in_both": len(l1), "steps": steps,
-            "l1_rho_median": float(np.median(l1)) if l1 else None, "l1_rho_max": float(np.max(l1)) if l1 else None}
+    finite = [(a, d) for a, d, st32, st64 in zip(out[32][0], out[64][0], out[32][1], out[64][1])
+              if st32 == 0 and st64 == 0 and torch.isfinite(a).all()]
+    # a grid with a non-positive density in either precision is on its way to blowing up (the
+    # unstable PLM+LLF instances at CFL 0.8): counted apart, not in the error statistics
+    l1 = [float(torch.mean(torch.abs(a - d))) for a, d in finite if float(a.min()) > 0 and float(d.min()) > 0]
+    return {"instances": len(sub), "finite_in_both": len(finite), "non_positive_density": len(finite) - len(l1),
+            "steps": steps, "l1_rho_median": float(np.median(l1)) if l1 else None,
+            "l1_rho_max": float(np.max(l1)) if l1 else None}
 
 
 def orszag_tang(n):

@@ -787,7 +787,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
   if constexpr (SCH == PPM && !CL && PpmStrip<G::RW, DIM>::K > 1) {
     // no boundary map on this tile: one thread per strip of K cells shares the stencil work
     constexpr int K = PpmStrip<G::RW, DIM>::K, NS = G::RW / K;
-    constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
+    constexpr int W = G::RW, H = G::RH;
     for (int e = tid; e < NS * H * NV; e += nth) {
       // strip-major order, the variables of a cell on consecutive threads: a warp's scalar
       // stores into the cell-interleaved level hit distinct banks
@@ -810,7 +810,7 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       }, erow);
     }
   } else {
-    constexpr int W = G::RW, H = G::RH, WW = G::WW, WH = G::WH;
+    constexpr int W = G::RW, H = G::RH;
     for (int e = tid; e < W * H * NV; e += nth) {
       const int s = e / (W * H), rem = e % (W * H);
       const int row = rem / W, col = rem % W;

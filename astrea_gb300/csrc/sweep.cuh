@@ -479,7 +479,9 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
         else tma_load_3d(stage, map, B::x0(s0, t0), s0 + G::W_BEG, 0, &s_bar);
         if (strip_tma) tma_load_3d(qs_box, a.qmaps + (AX * 2 + SB::TILE_ID), SB::x0(s0, t0), SB::y0(s0, t0), 0, &s_bar);
       }
-      __syncthreads();  // the barrier is initialised before anyone waits on it
+      // only warp 0 waits on the barrier: its lanes see thread 0's initialisation after a
+      // warp barrier; the other warps wait in the block barrier below
+      if (tid < 32) __syncwarp();
       if (!strip_tma) stage_strip();
       // one warp polls the barrier; the others sleep in the block barrier, which then
       // orders the copied data (visible to the polling warp) before their reads
@@ -526,8 +528,8 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       if (AX == 1) tma_load_3d(stage, map, B::x0(s0, t0), t0 - G::QT, 0, &s_bar);
       else tma_load_3d(stage, map, B::x0(s0, t0), s0 + G::Q_BEG, 0, &s_bar);
     }
-    __syncthreads();  // the barrier is initialised before anyone waits on it
-    const bool landed = tid < 32 ? mbar_wait_timed(&s_bar, 0, kCopyWaitNs) : true;  // one warp polls
+    if (tid < 32) __syncwarp();  // warp 0 polls the barrier after thread 0 initialised it
+    const bool landed = tid < 32 ? mbar_wait_timed(&s_bar, 0, kCopyWaitNs) : true;
     if (!__syncthreads_and(landed)) {
       // the copy did not complete in time: flag the grid, wait (bounded) for the copy, stop this tile
       if (tid == 0) {
@@ -579,7 +581,8 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
       }
     }
   }
-  __syncthreads();
+  // (read in place, the staged level was ordered by the copy's barrier already)
+  if constexpr (!W_IN_BOX) __syncthreads();
 
   // ---- level wS: cell-averaged primitives
   // (items laid out with the staged level's row pitch, so that a warp's loads
@@ -878,7 +881,9 @@ __device__ __forceinline__ void sweep_tile_body(const SweepArgs<T>& a, const int
     }
     if (a.want_emax) block_max_to_clock(lmax, &a.clock->emax[DIM == 1 ? 0 : AX]);
   }
-  __syncthreads();
+  // the face levels read the speeds only for LLF; otherwise this level writes no shared
+  // memory that they use (its block maximum keeps its own barrier)
+  if constexpr (LAM_ALL) __syncthreads();
 
   // per-interface solve from the six face arrays
   auto solve = [&](int k_local, int lam_row, const T* wSr, const T* wp, const T* wm, const T* qp, const T* qm,

@@ -111,7 +111,7 @@ def solver_of(solver, category=None):
     if category == "hll":
         return "hlld" if s.endswith("d") else "hllc"
     if category == "complete":
-        raise ConfigError(f"solver {solver!r} (Osher-Solomon / entropy-stable) is not provided by this build")
+        raise ConfigError(f"solver {solver!r} (Osher-Solomon / entropy-stable) is not provided by astrea_gb300")
     return "lw" if s.endswith("w") else "llf"
 
 

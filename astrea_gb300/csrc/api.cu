@@ -580,7 +580,7 @@ template <typename T> struct Engine final : IEngine {
     T* u = static_cast<T*>(state);
     if (cfg.integrator >= SSPRK53) return enqueue_step_rk(u, c, device_dt, st, tm);
     const int ns = stages_of(cfg.integrator);
-    if (ns < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this build");
+    if (ns < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this library");
     if (ct()) return enqueue_step_ct(u, c, device_dt, st, tm);
     const long long n = cells;
     const int threads = 256;
@@ -750,7 +750,7 @@ static int validate(const astrea_cfg* c) {
   if (c->precision != 32 && c->precision != 64) return fail(ASTREA_ERR_CONFIG, "precision must be 32 or 64");
   if (c->scheme < 0 || c->scheme > WENO7) return fail(ASTREA_ERR_CONFIG, "unknown scheme");
   if (c->solver < 0 || c->solver > LW) return fail(ASTREA_ERR_CONFIG, "unknown solver");
-  if (stages_of(c->integrator) < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this build");
+  if (stages_of(c->integrator) < 0) return fail(ASTREA_ERR_CONFIG, "integrator not supported by this library");
   if (c->boundary != EDGE && c->boundary != WRAP) return fail(ASTREA_ERR_CONFIG, "boundary must be edge(0) or wrap(1)");
   if ((c->flags & ASTREA_FLAG_CT) && (c->dim != 2 || c->model != 8))
     return fail(ASTREA_ERR_CONFIG, "constrained transport needs dim 2 and model 8");

@@ -56,14 +56,13 @@ WORKLOAD = "2D Euler shear layer 2048^2 periodic, PPM(mc) with flattening and ar
 SWEEP_DRAM_BYTES = 223.1e6
 SWEEP_DRAM_CELLS = 2048 * 2048
 # Floating-point operations per cell-update of one SSPRK3 step (every kernel of the step),
-# from ncu's SASS op counters (fadd + fmul + 2 x ffma, and the FP64 counterparts) over one
-# step of the workload at 512^2 (profiles/flops_step_2d_shear.md; counted on the build before
-# the packed FP32 pairs, whose operations are the same).  FP64 division and square
-# root are instruction sequences, which is why the FP64 step counts more operations.  The FP64
-# count was taken with the 32 x 8 FP64 tile; where the autotuner picks the 32 x 15 tile the step
-# recomputes fewer halo cells, so the reported FP64 fraction is an upper estimate.
-FLOPS_FP32_PER_CELL_UPDATE = 5005.1
-FLOPS_FP64_PER_CELL_UPDATE = 11979.3
+# from ncu's SASS op counters (fadd + fmul + 2 x ffma + 2 x fadd2 + 2 x fmul2 + 4 x ffma2, and
+# the FP64 counterparts) over one step of the workload at 512^2 (profiles/flops_step_2d_shear.md;
+# FP32 with the 32 x 8 tile along axis 0 and 32 x 15 along axis 1, FP64 with 32 x 15 on both).
+# FP64 division and square root are instruction sequences, which is why the FP64 step counts
+# more operations.
+FLOPS_FP32_PER_CELL_UPDATE = 4771.1
+FLOPS_FP64_PER_CELL_UPDATE = 11544.4
 # warp instructions per cell-update of the FP32 step (smsp__inst_executed.sum of every launch of a
 # step, launch list at 2048^2, profiles/sweep_kernel_f32_ppm_hllc_2d.md): against the issue rate of
 # one warp instruction per SM sub-partition per clock
